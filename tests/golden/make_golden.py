@@ -1,0 +1,96 @@
+"""Regenerate the golden fixtures from the reference's own CPU solver.
+
+Run in a container that has the reference sources (the GPU hosts do not):
+
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+
+For every case below it runs oracle/_ref/ref_harness (the reference's
+LBMSolver, built from source) for the listed step counts and stores the grid
+tables, the JSON ``solver`` block and the resulting populations, variables and
+residual in tests/golden/<case>_<steps>.npz.  The case configs are either the
+project's own JSON files in tests/golden/cases/ (written in the reference's
+config schema) or the reference's own test configs, read where they lie.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+REF = os.environ.get("LBM_REFERENCE_ROOT", "/root/reference")
+
+# (fixture name, config path, step counts)
+CASES = [
+    ("couette", ("ref", "test/couette/couette.json"), [1, 50]),
+    ("couette_bnd", ("ref", "test/couette/couette_bnd.json"), [1, 50]),
+    ("couette_bnd_bbDirichlet", ("ref", "test/couette/couette_bnd_bbDirichlet.json"), [50]),
+    ("couette_bnd_eq", ("ref", "test/couette/couette_bnd_eq.json"), [50]),
+    ("couette_bnd_eq2", ("ref", "test/couette/couette_bnd_eq2.json"), [50]),
+    ("couette_bnd_NEEM", ("ref", "test/couette/couette_bnd_NEEM.json"), [50]),
+    ("couette_bnd_NEBB", ("ref", "test/couette/couette_bnd_NEBB.json"), [50]),
+    ("poiseuille", ("ref", "test/poiseuille/poiseuille.json"), [1, 50]),
+    ("poiseuille_bnd", ("ref", "test/poiseuille/poiseuille_bnd.json"), [50]),
+    ("poiseuille_bnd_eq", ("ref", "test/poiseuille/poiseuille_bnd_eq.json"), [50]),
+    ("poiseuille_bnd_NEEM", ("ref", "test/poiseuille/poiseuille_bnd_NEEM.json"), [50]),
+    ("poiseuille_bnd_NEBB", ("ref", "test/poiseuille/poiseuille_bnd_NEBB.json"), [50]),
+    ("poiseuille_bnd_pressure", ("ref", "test/poiseuille/poiseuille_bnd_pressure.json"), [50]),
+    ("poiseuille_bnd_pressure_neem2", ("ref", "test/poiseuille/poiseuille_bnd_pressure_neem2.json"), [50]),
+    ("poisson1D_reaction", ("ref", "test/poisson/poisson1D_reaction.json"), [50]),
+    ("poisson1d_dh_small", ("own", "poisson1d_dh_small.json"), [1, 100]),
+    ("poisson2d_d2q5_small", ("own", "poisson2d_d2q5_small.json"), [1, 100]),
+    ("poisson2d_d2q9_reaction_small", ("own", "poisson2d_d2q9_reaction_small.json"), [100]),
+    ("poisson2d_helmholtz_small", ("own", "poisson2d_helmholtz_small.json"), [100]),
+    ("cavity_small", ("own", "cavity_small.json"), [1, 100]),
+    ("channel_mixed_small", ("own", "channel_mixed_small.json"), [1, 100]),
+]
+
+
+def config_path(src):
+    kind, rel = src
+    return os.path.join(REF, rel) if kind == "ref" else os.path.join(HERE, "cases", rel)
+
+
+def run_case(name, src, steps):
+    cfg_path = config_path(src)
+    with open(cfg_path) as fh:
+        cfg = json.load(fh)
+    with tempfile.TemporaryDirectory() as tmp:
+        # the harness writes logs into its working directory
+        local_cfg = os.path.join(tmp, "case.json")
+        with open(local_cfg, "w") as fh:
+            json.dump(cfg, fh)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        subprocess.run([HARNESS, local_cfg, str(steps), out], cwd=tmp, check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        with open(os.path.join(out, "meta.json")) as fh:
+            meta = json.load(fh)
+        arrays = {}
+        for key, dtype in (("centers", np.float64), ("nghbr", np.int64), ("fold0", np.float64), ("fold", np.float64),
+                           ("vars", np.float64), ("varsold", np.float64), ("residual", np.float64)):
+            arrays[key] = np.fromfile(os.path.join(out, f"{key}.{ 'i64' if dtype is np.int64 else 'f64'}"), dtype=dtype)
+    np.savez_compressed(os.path.join(HERE, f"{name}_{steps}.npz"), meta=json.dumps(meta), solver=json.dumps(cfg["solver"]),
+                        **arrays)
+    print(f"{name}_{steps}: {meta['cells']} cells")
+
+
+def main(argv):
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference first: oracle/build_ref.sh")
+    wanted = set(argv[1:])
+    for name, src, steps in CASES:
+        if wanted and name not in wanted:
+            continue
+        for n in steps:
+            run_case(name, src, n)
+
+
+if __name__ == "__main__":
+    main(sys.argv)
