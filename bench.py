@@ -1,0 +1,290 @@
+"""Benchmark of the GB300 LBM time step (one JSON line on rank 0).
+
+Workload (default): D3Q19 flow past a sphere, 512 x 256 x 256 cells, sphere of
+radius 24 at (128,128,128) voxelised on cell centres and bounced back,
+equilibrium velocity inlet u = 0.05 at x = 0, zero-gradient outlet at x = 511,
+free-slip side walls, BGK tau drawn from [0.52, 0.6] by seed.  Inputs are
+synthetic (built from the seed); the populations (1.3 GB in FP16, 5.1 GB in
+FP64) are larger than L2, so no flush is needed between steps.
+
+A "step" is one time step of the whole box.  ``value`` is MLUPS of the
+headline storage (FP16 deviations from the lattice weights, FP32 arithmetic)
+with the state resident in HBM; FP64 (the plain method), FP32 and BF16 are
+timed the same way and reported with their velocity L2 error against FP64.
+``e2e`` is the same metric through the C ABI with host buffers: the initial
+FP64 populations are copied from pinned host memory and every step's residual
+is read back to the host inside the timed region.
+
+--impl reference times the reference path on the host CPU.  The reference
+cannot run D3Q19 (its 3D neighbour table aborts, src/cartesiangrid.h:488-491),
+so its stand-in is the project's FP64 CPU restatement of the same step
+(oracle/, OpenMP over all host cores) on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+D3Q19 = 4
+B_PER_CELL = {"f64": 2 * 19 * 8 + 1, "f32": 2 * 19 * 4 + 1, "f16dev": 2 * 19 * 2 + 1, "bf16dev": 2 * 19 * 2 + 1}
+METRIC = "MLUPS (D3Q19 sphere 512x256x256, FP16-deviation storage)"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def sphere_case(nx=512, ny=256, nz=256, radius=24.0, center=(128.0, 128.0, 128.0), seed=2026):
+    rng = np.random.default_rng(seed)
+    tau = float(rng.uniform(0.52, 0.6))
+    flags = np.zeros((nz, ny, nx), dtype=np.uint8)
+    lo = [max(0, int(math.floor(c - radius - 1))) for c in center]
+    hi = [int(math.ceil(c + radius + 1)) for c in center]
+    z, y, x = np.meshgrid(np.arange(lo[2], min(hi[2], nz)), np.arange(lo[1], min(hi[1], ny)), np.arange(lo[0], min(hi[0], nx)),
+                          indexing="ij")
+    inside = (x + 0.5 - center[0]) ** 2 + (y + 0.5 - center[1]) ** 2 + (z + 0.5 - center[2]) ** 2 < radius * radius
+    sub = flags[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]]
+    sub[inside] = 1
+    flags[:, :, 0] = 2
+    flags[:, :, -1] = 3
+    return dict(shape=(nx, ny, nz), tau=tau, flags=flags.reshape(-1),
+                faces=("open", "open", "freeslip", "freeslip", "freeslip", "freeslip"), inlet=(0.05, 0.0, 0.0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"lbm_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(threads: int, budget_s: float = 12.0):
+    """The FP64 CPU restatement (oracle) on a bounded sample of the workload:
+    the same geometry scaled to 128 x 64 x 64 cells (sphere radius 6)."""
+    import oracle
+
+    case = sphere_case(128, 64, 64, radius=6.0, center=(32.0, 32.0, 32.0))
+    o = oracle.BoxOracle(D3Q19, case["shape"], 1.0 / case["tau"], faces=case["faces"], flags=case["flags"],
+                         inlet_velocity=case["inlet"])
+    o.init_equilibrium()
+    t0 = time.perf_counter()
+    o.step(2, threads)
+    dt = (time.perf_counter() - t0) / 2
+    steps = max(2, min(400, int(budget_s / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    o.step(steps, threads)
+    sec = time.perf_counter() - t0
+    cells = int(np.prod(case["shape"]))
+    return {"value": cells * steps / sec / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"D3Q19 sphere scaled to 128x64x64 (r=6), {steps} steps, FP64, OpenMP {threads} threads"}
+
+
+def run_variant(storage, case, warmup, steps, device):
+    from lbm_gb300.solver import BoxSolver
+
+    s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], storage, faces=case["faces"], flags=case["flags"],
+                  inlet_velocity=case["inlet"], device=device)
+    s.initial_condition()
+    s.step(warmup)
+    s.synchronize()
+    tot, ker, n = s.profile_steps(steps)
+    return s, tot, ker, n
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
+    ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(threads)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "D3Q19 flow past a sphere (CPU sample)", "sample": cb["sample"]},
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "vs_baseline": None}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = local
+    case = sphere_case()
+    cells = int(np.prod(case["shape"]))
+    hbm, peak_kind = peaks()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # headline storage, resident in HBM
+    barrier()
+    with ClockSampler(device) as clk:
+        s, tot_ms, ker_ms, launches = run_variant(args.storage, case, args.warmup, args.steps, device)
+    barrier()
+    t = torch.tensor([tot_ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    tot_ms = float(t.item())
+    mlups = cells * args.steps * world / (tot_ms / 1e3) / 1e6
+    kernel_avg_ms = ker_ms / launches
+    achieved = B_PER_CELL[args.storage] * cells / (kernel_avg_ms / 1e3) / 1e9
+    _, u_head = s.moments()
+    tpb = s.threads_per_block()
+    s.close()
+
+    # the plain FP64 method and the other storages, same steps from the same start
+    variants = {}
+    ref64, t64, k64, n64 = run_variant("f64", case, args.warmup, args.steps, device)
+    _, u64 = ref64.moments()
+    ref64.close()
+    variants["f64"] = {"mlups": cells * args.steps / (t64 / 1e3) / 1e6, "kernel_ms": k64 / n64}
+    err_head = float(np.linalg.norm(u_head - u64) / np.linalg.norm(u64))
+    del u_head
+    if not args.quick:
+        for st in ("f32", "bf16dev"):
+            if st == args.storage:
+                continue
+            v, tt, kk, nn = run_variant(st, case, args.warmup, args.steps, device)
+            _, uu = v.moments()
+            v.close()
+            variants[st] = {"mlups": cells * args.steps / (tt / 1e3) / 1e6, "kernel_ms": kk / nn,
+                            "vel_rel_l2_vs_f64": float(np.linalg.norm(uu - u64) / np.linalg.norm(u64))}
+            del uu
+    del u64
+
+    # end to end through the C ABI with host buffers
+    from lbm_gb300.solver import BoxSolver
+
+    e = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.storage, faces=case["faces"], flags=case["flags"],
+                  inlet_velocity=case["inlet"], device=device)
+    host = torch.empty((19, cells), dtype=torch.float64, pin_memory=True).numpy()
+    w = np.array([1 / 18] * 6 + [1 / 36] * 12 + [1 / 3])
+    host[:] = w[:, None]
+    e.set_populations(host)
+    e.step(args.warmup)
+    barrier()
+    t0 = time.perf_counter()
+    e.set_populations(host)  # H2D of the job's input state
+    for _ in range(args.steps):
+        e.step(1)
+        e.residual()  # D2H of the step's result
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    e.close()
+    e2e = {"value": cells * args.steps * world / wall / 1e6, "unit": "MLUPS",
+           "h2d_bytes_per_step": int(host.nbytes // args.steps), "d2h_bytes_per_step": 8 * 4}
+    del host
+
+    line = {
+        "metric": METRIC,
+        "value": mlups,
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": tot_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "D3Q19 flow past a sphere 512x256x256, r=24 at (128,128,128), eq. inlet u=0.05, zero-gradient outlet, "
+                               "free-slip sides", "tau": case["tau"], "storage": args.storage, "cells": cells,
+                   "bytes_per_cell": B_PER_CELL[args.storage], "l2": "state larger than L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "threads_per_block": tpb},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_box_step (AA step)", "kernel_avg_ms": kernel_avg_ms},
+        "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + args.steps},
+        "variants": variants,
+        "gpu_launches": int(launches * (2 if case["faces"][1] == "open" else 1)),
+        "e2e": e2e,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(threads)
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

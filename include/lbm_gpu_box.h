@@ -1,0 +1,101 @@
+/*
+ * lbm_gpu_box.h -- C ABI of the dense-box engine of the GB300 LBM library.
+ *
+ * The reference stores its uniform grid as a curve-ordered cell list with an
+ * int64 neighbour table (src/cartesiangrid.h:111-124).  For a uniform box the
+ * same time step (LBMSolver::timeStep, src/lbm/solver.cpp:306-320) needs no
+ * table at all: neighbours follow from coordinates, and a flag byte per cell
+ * (fluid / solid / inlet / outlet / Dirichlet) carries the geometry.  This
+ * header is the entry point for that layout: it is what the reference's
+ * LBMSolver calls when its grid is a single uniform level (every test case
+ * and every synthetic benchmark domain), and it is the only form in which the
+ * features the reference lacks are available (D3Q19, D3Q7 Poisson-Boltzmann,
+ * Guo body forcing, equilibrium inlet, zero-gradient outlet, free slip,
+ * reduced-precision storage).
+ *
+ * Populations live on the device as q-major planes in the chosen storage and
+ * stream in place with the AA pattern.  Transfers use FP64 SoA host arrays:
+ * f[q * ncells + cell], cell = x + nx * (y + ny * z).  The context type and
+ * every other entry point (step, residual, mass/momentum, destroy, errors) are
+ * those of lbm_gpu.h.
+ */
+#ifndef LBM_GPU_BOX_H
+#define LBM_GPU_BOX_H
+
+#include <stdint.h>
+
+#include "lbm_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* population storage */
+typedef enum lbm_storage {
+  LBM_STORE_F64     = 0, /* FP64 populations, FP64 arithmetic (the plain method) */
+  LBM_STORE_F32     = 1, /* FP32 populations, FP32 arithmetic */
+  LBM_STORE_F16_DEV = 2, /* FP16 of (f_i - w_i) / w_i * 2^12, FP32 arithmetic */
+  LBM_STORE_BF16_DEV = 3 /* BF16 of the same scaled deviation, FP32 arithmetic */
+} lbm_storage;
+
+/* treatment of a face of the box */
+typedef enum lbm_face {
+  LBM_FACE_WALL     = 0, /* halfway bounce-back, optionally moving (wall_velocity) */
+  LBM_FACE_PERIODIC = 1, /* wrap to the opposite face (both faces of the axis) */
+  LBM_FACE_FREESLIP = 2, /* specular reflection */
+  LBM_FACE_OPEN     = 3  /* -x: equilibrium inlet plane, +x: zero-gradient outlet plane */
+} lbm_face;
+
+/* per-cell flag byte */
+typedef enum lbm_cell_flag {
+  LBM_CELL_FLUID     = 0,
+  LBM_CELL_SOLID     = 1, /* bounce-back obstacle, not updated */
+  LBM_CELL_INLET     = 2, /* emits the equilibrium at (inlet_density, inlet_velocity) */
+  LBM_CELL_OUTLET    = 3, /* fluid cell whose links from beyond +x copy the upstream cell */
+  LBM_CELL_DIRICHLET = 4  /* Poisson: emits the equilibrium at its fixed potential */
+} lbm_cell_flag;
+
+typedef struct lbm_box_desc {
+  int32_t lattice;          /* LBM_D2Q9, LBM_D3Q19 (Navier-Stokes) or LBM_D3Q7 (Poisson-Boltzmann) */
+  int32_t equation;         /* LBM_NAVIER_STOKES or LBM_POISSON */
+  int32_t storage;          /* lbm_storage */
+  int32_t device;
+  int32_t nx, ny, nz;       /* nz = 1 for D2Q9 */
+  int32_t face[6];          /* lbm_face of -x,+x,-y,+y,-z,+z */
+  double  omega;            /* 1/tau */
+  double  wall_velocity[6][3];
+  double  body_force[3];    /* Guo forcing, lattice units */
+  double  inlet_density;
+  double  inlet_velocity[3];
+  double  init_density;     /* initial equilibrium */
+  double  init_velocity[3];
+  double  kappa_sq;         /* Poisson-Boltzmann: nabla^2 phi = kappa^2 sinh(phi) (or kappa^2 phi) */
+  int32_t pb_nonlinear;     /* 1: sinh, 0: linear Debye-Hueckel */
+  int32_t reserved;
+} lbm_box_desc;
+
+/* flags: ncells bytes (NULL = all fluid); dirichlet: ncells potentials of the
+ * LBM_CELL_DIRICHLET cells (Poisson) or NULL. */
+int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const double* dirichlet, lbm_gpu_ctx** out);
+
+/* Macroscopic fields of the current state, FP64 host arrays of ncells:
+ * rho (or phi for Poisson) and ux, uy, uz (NULL to skip). */
+int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, double* uz);
+
+/* Launch configuration chosen by the autotuner (threads per block) and a
+ * request to re-run it. */
+int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
+
+/* Run nsteps exactly as lbm_gpu_step does, but with a CUDA event pair around
+ * every launch of the step kernel on the context's stream: total_ms is the
+ * device time of the whole sequence, kernel_ms the summed duration of the
+ * step-kernel launches, launches their count (any pointer may be NULL). */
+int lbm_gpu_box_profile_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* total_ms, double* kernel_ms, int64_t* launches);
+
+/* Bytes of one population in the chosen storage. */
+int lbm_gpu_box_storage_bytes(int32_t storage);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1137 @@
+// Dense-box engine: BGK / Poisson-Boltzmann step on a structured box, AA-pattern
+// in-place streaming, FP64 / FP32 / FP16 / BF16 population storage.
+//
+// Physics per cell is the reference's BGK update (src/lbm/solver.cpp:512-622:
+// moments, equilibrium eq::defaultEq, f = (1-omega) f + omega feq) with, where
+// requested, Guo body forcing, and for D3Q7 the Chai-Shi Poisson collision of
+// src/lbm/solver.cpp:589-611 with a sinh source.
+//
+// Streaming (the reference's push propagationStep, solver.cpp:714-740, plus its
+// halfway bounce-back at wet-node boundary rows, bnd_dirichlet.h:79-121) uses
+// the AA pattern: one population array, updated in place.
+//   even step: cell x reads its own slots A[q][x], collides, writes the
+//              post-collision value of direction q to A[opp(q)][x];
+//   odd step:  cell x pulls f_q from A[opp(q)][x - c_q], collides, and pushes
+//              the result of direction q to A[q][x + c_q].
+// Every location is read and then written by the same thread, so the update is
+// race-free without a second array.  Walls, solids, free slip, periodic wrap and
+// the inlet/outlet planes are resolved per link: the pull side asks "which
+// post-collision population arrives here" (src()), the push side asks "where
+// does the population leaving here land" (dst()); the two are inverses.
+//
+// Storage: FP64 stores f; FP32 stores f - w; FP16 / BF16 store (f - w)/w * 2^12
+// (the lattice weights make every direction's deviation O(1) before scaling,
+// and the power-of-two scale keeps small deviations out of the subnormal
+// range).  Arithmetic is FP64 for FP64 storage and FP32 otherwise; Navier-Stokes
+// in reduced precision works on deviations from the weights throughout.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "box.h"
+#include "lattice.cuh"
+
+namespace lbm {
+namespace {
+
+constexpr uint8_t TYPE_MASK  = 0x07;
+constexpr uint8_t NEAR_SOLID = 0x08;  // set by the engine: a neighbour is solid
+constexpr float   DEV_SCALE  = 4096.0f;
+
+// ---- storage conversions ---------------------------------------------------
+template <int ST>
+struct Store;
+template <>
+struct Store<LBM_STORE_F64> {
+  using T = double;
+  using C = double;
+  static constexpr bool DEV = false;
+  static __device__ __forceinline__ C load(T v, C) { return v; }
+  static __device__ __forceinline__ T store(C f, C) { return f; }
+};
+template <>
+struct Store<LBM_STORE_F32> {
+  using T = float;
+  using C = float;
+  static constexpr bool DEV = true;  // holds f - w
+  static __device__ __forceinline__ C load(T v, C) { return v; }
+  static __device__ __forceinline__ T store(C d, C) { return d; }
+};
+template <>
+struct Store<LBM_STORE_F16_DEV> {
+  using T = __half;
+  using C = float;
+  static constexpr bool DEV = true;
+  // deviation d = w * h / 2^12
+  static __device__ __forceinline__ C load(T v, C w) { return __half2float(v) * (w * (1.0f / DEV_SCALE)); }
+  static __device__ __forceinline__ T store(C d, C w) { return __float2half_rn(d * (DEV_SCALE / w)); }
+};
+template <>
+struct Store<LBM_STORE_BF16_DEV> {
+  using T = __nv_bfloat16;
+  using C = float;
+  static constexpr bool DEV = true;
+  static __device__ __forceinline__ C load(T v, C w) { return __bfloat162float(v) * (w * (1.0f / DEV_SCALE)); }
+  static __device__ __forceinline__ T store(C d, C w) { return __float2bfloat16_rn(d * (DEV_SCALE / w)); }
+};
+
+// ---- link resolution ---------------------------------------------------------
+// mirror of direction q in the axes of `mask` (free-slip reflection)
+template <int LAT>
+__device__ __forceinline__ int mirror(int q, int mask) {
+  using L = Lattice<LAT>;
+  int c[3] = {L::c(q, 0), L::c(q, 1), L::c(q, 2)};
+#pragma unroll
+  for(int a = 0; a < 3; ++a)
+    if(mask & (1 << a)) c[a] = -c[a];
+#pragma unroll
+  for(int k = 0; k < L::Q; ++k)
+    if(L::c(k, 0) == c[0] && L::c(k, 1) == c[1] && L::c(k, 2) == c[2]) return k;
+  return q;
+}
+
+enum LinkKind { LINK_CELL = 0, LINK_BOUNCE = 1, LINK_OPEN = 2 };
+
+struct Link {
+  int     kind;
+  int64_t cell;  // LINK_CELL: cell to read / write
+  int     q;     // LINK_CELL: direction of the population at that cell
+  double  corr;  // LINK_BOUNCE: moving-wall momentum added to the arriving population
+};
+
+// Resolve the cell reached from (x,y,z) by displacement sign*c_q, through
+// the box faces.  sign=-1: source of the population arriving at (x,y,z) in
+// direction q; sign=+1: destination of the population leaving it.
+// `arrive` is the direction of the population that arrives at (x,y,z) when the
+// link bounces back (q for the pull side, opp(q) for the push side).
+template <int LAT>
+__device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z, int q, int sign, int arrive) {
+  using L       = Lattice<LAT>;
+  const int n[3] = {P.nx, P.ny, P.nz};
+  int       p[3] = {x, y, z};
+  int       s[3];
+  int       mask = 0;
+  bool      bb = false, open = false;
+  double    corr = 0.0;
+#pragma unroll
+  for(int a = 0; a < L::D; ++a) {
+    s[a] = p[a] + sign * L::c(q, a);
+    if(s[a] < 0 || s[a] >= n[a]) {
+      const int face = s[a] < 0 ? 2 * a : 2 * a + 1;
+      const int ft   = P.face[face];
+      if(ft == LBM_FACE_PERIODIC) {
+        s[a] = s[a] < 0 ? s[a] + n[a] : s[a] - n[a];
+      } else if(ft == LBM_FACE_FREESLIP) {
+        s[a] = p[a];
+        mask |= 1 << a;
+      } else if(ft == LBM_FACE_OPEN) {
+        open = true;
+      } else {
+        bb = true;
+        double cu = 0;
+#pragma unroll
+        for(int d = 0; d < L::D; ++d) cu += static_cast<double>(L::c(arrive, d)) * P.wall_u[face][d];
+        corr += 6.0 * L::w(arrive) * cu;  // 2 w (c.u_w) / c_s^2 with rho_w = 1
+      }
+    }
+  }
+#pragma unroll
+  for(int a = L::D; a < 3; ++a) s[a] = 0;
+  if(open) return Link{LINK_OPEN, 0, q, 0.0};
+  if(bb) return Link{LINK_BOUNCE, 0, q, corr};
+  const int64_t cell = s[0] + static_cast<int64_t>(P.nx) * (s[1] + static_cast<int64_t>(P.ny) * s[2]);
+  if((P.flags[cell] & TYPE_MASK) == LBM_CELL_SOLID) return Link{LINK_BOUNCE, 0, q, 0.0};
+  return Link{LINK_CELL, cell, mask ? mirror<LAT>(q, mask) : q, 0.0};
+}
+
+template <int LAT>
+__device__ __forceinline__ int64_t offset(const BoxParams& P, int q) {
+  using L = Lattice<LAT>;
+  return L::c(q, 0) + static_cast<int64_t>(P.nx) * (L::c(q, 1) + static_cast<int64_t>(P.ny) * L::c(q, 2));
+}
+
+template <int LAT>
+__device__ __forceinline__ bool interior(const BoxParams& P, int x, int y, int z) {
+  using L = Lattice<LAT>;
+  bool in = x > 0 && x < P.nx - 1;
+  if(L::D > 1) in = in && y > 0 && y < P.ny - 1;
+  if(L::D > 2) in = in && z > 0 && z < P.nz - 1;
+  return in;
+}
+
+// outlet ghost: value of direction q (c_qx = -1) for the outlet cell (y,z)
+__device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y, int z) {
+  return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
+}
+
+// ---- collision -------------------------------------------------------------
+// f (or its deviation from w for DEV storage) in, post-collision out
+template <int LAT, int EQ, class C, bool DEV>
+__device__ __forceinline__ void collide(const BoxParams& P, C* f, int64_t cell, C* mom_out) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  const C       omega = static_cast<C>(P.omega);
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    C rho0 = 0, j[3] = {0, 0, 0};
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      rho0 += f[q];
+#pragma unroll
+      for(int d = 0; d < D; ++d) {
+        if(L::c(q, d) > 0) j[d] += f[q];
+        if(L::c(q, d) < 0) j[d] -= f[q];
+      }
+    }
+    // DEV: rho0 is rho - 1 (sum of deviations), j is exact since sum c w = 0
+    const C rho  = DEV ? C(1) + rho0 : rho0;
+    const C irho = C(1) / rho;
+    C       u[3] = {0, 0, 0};
+    C       F[3] = {0, 0, 0};
+    if(P.has_force) {
+#pragma unroll
+      for(int d = 0; d < D; ++d) F[d] = static_cast<C>(P.force[d]);
+    }
+#pragma unroll
+    for(int d = 0; d < D; ++d) u[d] = (j[d] + C(0.5) * F[d]) * irho;
+    C usq = 0;
+#pragma unroll
+    for(int d = 0; d < D; ++d) usq += u[d] * u[d];
+    if(mom_out) {
+      mom_out[0] = rho;
+#pragma unroll
+      for(int d = 0; d < D; ++d) mom_out[1 + d] = u[d];
+    }
+    const C guo = C(1) - C(0.5) * omega;
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      C cu = 0;
+#pragma unroll
+      for(int d = 0; d < D; ++d) {
+        if(L::c(q, d) > 0) cu += u[d];
+        if(L::c(q, d) < 0) cu -= u[d];
+      }
+      const C w = static_cast<C>(L::w(q));
+      // feq - w = w (rho - 1 + rho (3 cu + 4.5 cu^2 - 1.5 u^2)) for DEV storage
+      const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
+      C       feq;
+      if(DEV) feq = w * (rho0 + rho * poly);
+      else feq = w * rho * (C(1) + poly);
+      C out = f[q] + omega * (feq - f[q]);
+      if(P.has_force) {
+        C cf = 0, uf = 0;
+#pragma unroll
+        for(int d = 0; d < D; ++d) {
+          cf += static_cast<C>(L::c(q, d)) * F[d];
+          uf += u[d] * F[d];
+        }
+        out += guo * w * (C(3) * (cf - uf) + C(9) * cu * cf);
+      }
+      f[q] = out;
+    }
+  } else {
+    // Poisson(-Boltzmann), Chai & Shi: phi from the moving populations
+    C acc = 0;
+#pragma unroll
+    for(int q = 0; q < Q - 1; ++q) acc += f[q];
+    const C phi = acc * static_cast<C>(1.0 / (1.0 - L::w(Q - 1)));
+    if(mom_out) mom_out[0] = phi;
+    const C g   = P.pb_nonlinear ? static_cast<C>(sinh(static_cast<double>(phi))) : phi;
+    const C src = static_cast<C>(P.pb_diffusivity * P.kappa_sq) * g;
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      const C feq = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+      C       out = f[q] + omega * (feq - f[q]);
+      if(q != Q - 1) out += static_cast<C>(L::pw(q)) * src;
+      f[q] = out;
+    }
+  }
+}
+
+// equilibrium emitted by inlet / Dirichlet cells (deviation for DEV storage)
+template <int LAT, int EQ, class C, bool DEV>
+__device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* f, int64_t cell) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    const C rho = static_cast<C>(P.inlet_rho);
+    C       usq = 0;
+#pragma unroll
+    for(int d = 0; d < D; ++d) usq += static_cast<C>(P.inlet_u[d] * P.inlet_u[d]);
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      C cu = 0;
+#pragma unroll
+      for(int d = 0; d < D; ++d) cu += static_cast<C>(L::c(q, d)) * static_cast<C>(P.inlet_u[d]);
+      const C w    = static_cast<C>(L::w(q));
+      const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
+      f[q]         = DEV ? w * ((rho - C(1)) + rho * poly) : w * rho * (C(1) + poly);
+    }
+  } else {
+    const C phi = P.dirichlet ? static_cast<C>(P.dirichlet[cell]) : C(0);
+#pragma unroll
+    for(int q = 0; q < Q; ++q) f[q] = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---- the step kernel ---------------------------------------------------------
+// MOM: 0 plain, 1 also write the moments, 2 also accumulate |moments - previous|
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+__global__ void __launch_bounds__(512) k_box_step(BoxParams P) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q, D = L::D;
+  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
+  constexpr int NV   = EQ == LBM_NAVIER_STOKES ? D + 1 : 1;
+
+  const int  x     = blockIdx.x * blockDim.x + threadIdx.x;
+  const int  y     = blockIdx.y;
+  const int  z     = blockIdx.z;
+  const bool valid = x < P.nx;
+  const int64_t cell = valid ? x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z) : 0;
+  const uint8_t flag = valid ? P.flags[cell] : LBM_CELL_SOLID;
+  const uint8_t type = flag & TYPE_MASK;
+  T*            A    = static_cast<T*>(P.pop);
+  const int64_t NA   = P.nalloc;
+  double        diff[NV];
+#pragma unroll
+  for(int k = 0; k < NV; ++k) diff[k] = 0.0;
+
+  if(type != LBM_CELL_SOLID) {
+    C f[Q];
+    C mom[NV];
+    if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
+      emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+#pragma unroll
+      for(int k = 0; k < NV; ++k) mom[k] = 0;
+    } else {
+      const bool fast = !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+      if(!ODD) {
+#pragma unroll
+        for(int q = 0; q < Q; ++q) f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q)));
+        if(type == LBM_CELL_OUTLET) {
+          // links from beyond +x: what the upstream cell received (ghost)
+#pragma unroll
+          for(int q = 0; q < Q; ++q)
+            if(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
+        }
+      } else if(fast) {
+#pragma unroll
+        for(int q = 0; q < Q; ++q) f[q] = S::load(A[L::opp(q) * NA + cell - offset<LAT>(P, q)], static_cast<C>(L::w(q)));
+      } else {
+#pragma unroll
+        for(int q = 0; q < Q; ++q) {
+          const Link lk = resolve<LAT>(P, x, y, z, q, -1, q);
+          if(lk.kind == LINK_CELL) {
+            f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], static_cast<C>(L::w(q)));
+          } else if(lk.kind == LINK_BOUNCE) {
+            f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr);
+          } else {
+            f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
+          }
+        }
+      }
+      collide<LAT, EQ, C, DEV>(P, f, cell, MOM ? mom : nullptr);
+    }
+    if constexpr(MOM != 0) {
+      C* M = static_cast<C*>(P.mom);
+#pragma unroll
+      for(int k = 0; k < NV; ++k) {
+        if(MOM == 2) diff[k] = fabs(static_cast<double>(mom[k]) - static_cast<double>(M[k * P.ncells + cell]));
+        M[k * P.ncells + cell] = mom[k];
+      }
+    }
+    // write back
+    if(!ODD) {
+#pragma unroll
+      for(int q = 0; q < Q; ++q) A[L::opp(q) * NA + cell] = S::store(f[q], static_cast<C>(L::w(L::opp(q))));
+    } else {
+      const bool fast = !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+      if(fast) {
+#pragma unroll
+        for(int q = 0; q < Q; ++q) A[q * NA + cell + offset<LAT>(P, q)] = S::store(f[q], static_cast<C>(L::w(q)));
+      } else {
+#pragma unroll
+        for(int q = 0; q < Q; ++q) {
+          const Link lk = resolve<LAT>(P, x, y, z, q, +1, L::opp(q));
+          if(lk.kind == LINK_CELL) {
+            A[lk.q * NA + lk.cell] = S::store(f[q], static_cast<C>(L::w(lk.q)));
+          } else if(lk.kind == LINK_BOUNCE) {
+            const int o       = L::opp(q);
+            A[o * NA + cell] = S::store(f[q] + static_cast<C>(lk.corr), static_cast<C>(L::w(o)));
+          }
+          // LINK_OPEN: the population leaves the box
+        }
+      }
+    }
+  }
+  if constexpr(MOM == 2) {
+    __shared__ double red[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for(int k = 0; k < NV; ++k) {
+      const double s = warp_sum(diff[k]);
+      if(lane == 0) red[k][wid] = s;
+    }
+    __syncthreads();
+    if(wid == 0) {
+      const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
+      const int64_t nb = static_cast<int64_t>(gridDim.x) * gridDim.y * gridDim.z;
+#pragma unroll
+      for(int k = 0; k < NV; ++k) {
+        double s = lane < nw ? red[k][lane] : 0.0;
+        s        = warp_sum(s);
+        if(lane == 0) P.partials[k * nb + b] = s;
+      }
+    }
+  }
+}
+
+// outlet ghost fill, run before every step: for each outlet cell and each
+// direction q with c_qx = -1, the population its upstream neighbour receives
+template <int LAT, int ST, bool ODD>
+__global__ void k_box_outlet(BoxParams P) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  constexpr int Q = L::Q;
+  const int     y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int     z = blockIdx.y;
+  if(y >= P.ny) return;
+  const int     x  = P.nx - 1;
+  const int64_t r  = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
+  if((P.flags[r] & TYPE_MASK) != LBM_CELL_OUTLET) return;
+  T*            A  = static_cast<T*>(P.pop);
+  const int64_t NA = P.nalloc;
+  const int64_t u  = r - 1;
+#pragma unroll
+  for(int q = 0; q < Q; ++q) {
+    if(L::c(q, 0) >= 0) continue;
+    T v;
+    if(!ODD) {
+      v = A[q * NA + u];  // standard layout: what u received in the last odd step
+    } else {
+      const Link lk = resolve<LAT>(P, x - 1, y, z, q, -1, q);
+      if(lk.kind == LINK_CELL) {
+        v = A[L::opp(lk.q) * NA + lk.cell];
+      } else {
+        // bounce-back at the upstream cell (a wall or solid beside it)
+        using C = typename S::C;
+        v = S::store(S::load(A[q * NA + u], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr), static_cast<C>(L::w(q)));
+      }
+    }
+    A[Q * NA + ghost_index(P, q, y, z)] = v;
+  }
+}
+
+// FP64 post-stream populations of the current state (reference layout of
+// m_fold per cell), q-major, plus inlet/Dirichlet cells reported as the
+// equilibrium they emit and solids as zero
+template <int LAT, int EQ, int ST>
+__global__ void k_box_readout(BoxParams P, bool odd, double* out) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if(x >= P.nx) return;
+  const int64_t cell = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
+  const uint8_t type = P.flags[cell] & TYPE_MASK;
+  const T*      A    = static_cast<const T*>(P.pop);
+  const int64_t NA   = P.nalloc, N = P.ncells;
+  C             f[Q];
+  if(type == LBM_CELL_SOLID) {
+#pragma unroll
+    for(int q = 0; q < Q; ++q) out[q * N + cell] = 0.0;
+    return;
+  }
+  if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
+    emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+  } else {
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      const C w = static_cast<C>(L::w(q));
+      if(!odd) {
+        f[q] = S::load(A[q * NA + cell], w);
+        if(type == LBM_CELL_OUTLET && L::c(q, 0) < 0) f[q] = S::load(A[q * NA + cell - 1], w);
+      } else {
+        int  xs = x;
+        Link lk = resolve<LAT>(P, x, y, z, q, -1, q);
+        if(lk.kind == LINK_OPEN) {  // beyond the outlet: what the upstream cell receives
+          xs = x - 1;
+          lk = resolve<LAT>(P, xs, y, z, q, -1, q);
+        }
+        const int64_t own = xs + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
+        if(lk.kind == LINK_CELL) f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], w);
+        else f[q] = S::load(A[q * NA + own], w) + static_cast<C>(lk.corr);
+      }
+    }
+  }
+#pragma unroll
+  for(int q = 0; q < Q; ++q) out[q * N + cell] = static_cast<double>(f[q]) + (DEV ? L::w(q) : 0.0);
+}
+
+// store FP64 post-stream populations into the standard (even-parity) layout
+template <int LAT, int EQ, int ST>
+__global__ void k_box_load(BoxParams P, const double* in) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
+  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if(cell >= P.ncells) return;
+  T* A = static_cast<T*>(P.pop);
+#pragma unroll
+  for(int q = 0; q < Q; ++q) {
+    const double v = in[q * P.ncells + cell] - (DEV ? L::w(q) : 0.0);
+    A[q * P.nalloc + cell] = S::store(static_cast<C>(v), static_cast<C>(L::w(q)));
+  }
+}
+
+// uniform initial state: the same FP64 population vector in every cell
+struct InitVec {
+  double f[19];
+};
+template <int LAT, int EQ, int ST>
+__global__ void k_box_init(BoxParams P, InitVec v) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
+  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if(cell >= P.ncells) return;
+  T* A = static_cast<T*>(P.pop);
+#pragma unroll
+  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(v.f[q] - (DEV ? L::w(q) : 0.0)), static_cast<C>(L::w(q)));
+}
+
+// moments (rho or phi, u) of FP64 populations
+template <int LAT, int EQ>
+__global__ void k_box_moments_f64(BoxParams P, const double* f, double* rho, double* ux, double* uy, double* uz) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if(cell >= P.ncells) return;
+  const int64_t N = P.ncells;
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    double r = 0, j[3] = {0, 0, 0};
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      const double v = f[q * N + cell];
+      r += v;
+#pragma unroll
+      for(int d = 0; d < D; ++d) j[d] += L::c(q, d) * v;
+    }
+    const double F[3] = {P.has_force ? P.force[0] : 0.0, P.has_force ? P.force[1] : 0.0, P.has_force ? P.force[2] : 0.0};
+    if(rho) rho[cell] = r;
+    double* uu[3] = {ux, uy, uz};
+#pragma unroll
+    for(int d = 0; d < D; ++d)
+      if(uu[d]) uu[d][cell] = r != 0.0 ? (j[d] + 0.5 * F[d]) / r : 0.0;
+  } else {
+    double acc = 0;
+#pragma unroll
+    for(int q = 0; q < Q - 1; ++q) acc += f[q * N + cell];
+    if(rho) rho[cell] = acc / (1.0 - L::w(Q - 1));
+  }
+}
+
+__global__ void k_mark_near_solid(uint8_t* flags, int nx, int ny, int nz, int dims) {
+  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t n    = static_cast<int64_t>(nx) * ny * nz;
+  if(cell >= n) return;
+  const int x = static_cast<int>(cell % nx), y = static_cast<int>((cell / nx) % ny), z = static_cast<int>(cell / (static_cast<int64_t>(nx) * ny));
+  bool near = false;
+  for(int dz = (dims > 2 ? -1 : 0); dz <= (dims > 2 ? 1 : 0); ++dz)
+    for(int dy = (dims > 1 ? -1 : 0); dy <= (dims > 1 ? 1 : 0); ++dy)
+      for(int dx = -1; dx <= 1; ++dx) {
+        const int xx = x + dx, yy = y + dy, zz = z + dz;
+        if(xx < 0 || yy < 0 || zz < 0 || xx >= nx || yy >= ny || zz >= nz) continue;
+        if((flags[xx + static_cast<int64_t>(nx) * (yy + static_cast<int64_t>(ny) * zz)] & TYPE_MASK) == LBM_CELL_SOLID) near = true;
+      }
+  flags[cell] = static_cast<uint8_t>((flags[cell] & TYPE_MASK) | (near ? NEAR_SOLID : 0));
+}
+
+// sum over cells of the FP64 populations: mass and momentum
+template <int LAT>
+__global__ void k_box_sum(const double* f, int64_t n, double* partials) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  __shared__ double sh[D + 1][32];
+  double acc[D + 1];
+#pragma unroll
+  for(int k = 0; k <= D; ++k) acc[k] = 0;
+  for(int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+#pragma unroll
+    for(int q = 0; q < Q; ++q) {
+      const double v = f[q * n + i];
+      acc[0] += v;
+#pragma unroll
+      for(int d = 0; d < D; ++d) acc[d + 1] += L::c(q, d) * v;
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for(int k = 0; k <= D; ++k) {
+    const double s = warp_sum(acc[k]);
+    if(lane == 0) sh[k][wid] = s;
+  }
+  __syncthreads();
+  if(wid == 0) {
+#pragma unroll
+    for(int k = 0; k <= D; ++k) {
+      double s = lane < nw ? sh[k][lane] : 0.0;
+      s        = warp_sum(s);
+      if(lane == 0) partials[k * gridDim.x + blockIdx.x] = s;
+    }
+  }
+}
+
+__global__ void k_final_sum(const double* partials, int64_t nb, int nvec, double* out) {
+  __shared__ double sh[32];
+  for(int v = 0; v < nvec; ++v) {
+    double acc = 0;
+    for(int64_t i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[v * nb + i];
+    acc = warp_sum(acc);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if(lane == 0) sh[wid] = acc;
+    __syncthreads();
+    if(wid == 0) {
+      double s = lane < static_cast<int>(blockDim.x >> 5) ? sh[lane] : 0.0;
+      s        = warp_sum(s);
+      if(lane == 0) out[v] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+dim3 step_grid(const BoxState* b, int tpb) {
+  return dim3(static_cast<unsigned>((b->p.nx + tpb - 1) / tpb), static_cast<unsigned>(b->p.ny), static_cast<unsigned>(b->p.nz));
+}
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+  const int  tpb = b->tuned_tpb;
+  const dim3 g   = step_grid(b, tpb);
+  if(b->p.has_outlet) {
+    const dim3 go(static_cast<unsigned>((b->p.ny + 127) / 128), static_cast<unsigned>(b->p.nz));
+    if(odd) k_box_outlet<LAT, ST, true><<<go, 128, 0, s>>>(b->p);
+    else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p);
+  }
+  if(ev0) cudaEventRecord(ev0, s);
+  if(odd) {
+    if(mom == 0) k_box_step<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
+    else if(mom == 1) k_box_step<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
+    else k_box_step<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
+  } else {
+    if(mom == 0) k_box_step<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
+    else if(mom == 1) k_box_step<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
+    else k_box_step<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
+  }
+  if(ev1) cudaEventRecord(ev1, s);
+  return cudaGetLastError();
+}
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_readout(BoxState* b, double* out, cudaStream_t s) {
+  const dim3 g = step_grid(b, 128);
+  k_box_readout<LAT, EQ, ST><<<g, 128, 0, s>>>(b->p, (b->steps & 1) != 0, out);
+  return cudaGetLastError();
+}
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_load(BoxState* b, const double* in, cudaStream_t s) {
+  k_box_load<LAT, EQ, ST><<<static_cast<unsigned>((b->p.ncells + 255) / 256), 256, 0, s>>>(b->p, in);
+  return cudaGetLastError();
+}
+
+// one switch for every (lattice, equation, storage) instantiation
+#define LBM_BOX_DISPATCH(FN, ...)                                                                          \
+  do {                                                                                                     \
+    const int key = b->desc.lattice * 100 + b->desc.equation * 10 + b->desc.storage;                        \
+    switch(key) {                                                                                          \
+      case LBM_D2Q9 * 100 + 0 + LBM_STORE_F64: return FN<LBM_D2Q9, 0, LBM_STORE_F64>(__VA_ARGS__);         \
+      case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return FN<LBM_D2Q9, 0, LBM_STORE_F32>(__VA_ARGS__);         \
+      case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return FN<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(__VA_ARGS__); \
+      case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return FN<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(__VA_ARGS__); \
+      case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return FN<LBM_D3Q19, 0, LBM_STORE_F64>(__VA_ARGS__);       \
+      case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return FN<LBM_D3Q19, 0, LBM_STORE_F32>(__VA_ARGS__);       \
+      case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return FN<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(__VA_ARGS__); \
+      case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return FN<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(__VA_ARGS__); \
+      case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return FN<LBM_D3Q7, 1, LBM_STORE_F64>(__VA_ARGS__);        \
+      case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return FN<LBM_D3Q7, 1, LBM_STORE_F32>(__VA_ARGS__);        \
+      default: return cudaErrorInvalidValue;                                                               \
+    }                                                                                                      \
+  } while(0)
+
+cudaError_t dispatch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr) {
+  LBM_BOX_DISPATCH(launch_step, b, odd, mom, s, ev0, ev1);
+}
+cudaError_t dispatch_readout(BoxState* b, double* out, cudaStream_t s) { LBM_BOX_DISPATCH(launch_readout, b, out, s); }
+cudaError_t dispatch_load(BoxState* b, const double* in, cudaStream_t s) { LBM_BOX_DISPATCH(launch_load, b, in, s); }
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_init(BoxState* b, const InitVec& v, cudaStream_t s) {
+  k_box_init<LAT, EQ, ST><<<static_cast<unsigned>((b->p.ncells + 255) / 256), 256, 0, s>>>(b->p, v);
+  return cudaGetLastError();
+}
+cudaError_t dispatch_init(BoxState* b, const InitVec& v, cudaStream_t s) { LBM_BOX_DISPATCH(launch_init, b, v, s); }
+
+int64_t nblocks_step(const BoxState* b) {
+  const dim3 g = step_grid(b, b->tuned_tpb);
+  return static_cast<int64_t>(g.x) * g.y * g.z;
+}
+
+bool ensure_staging(BoxState* b) {
+  if(b->f64) return true;
+  return cudaMalloc(&b->f64, sizeof(double) * b->Q * b->p.ncells) == cudaSuccess;
+}
+
+int cerr(std::string& err, cudaError_t e, const char* what) {
+  err = std::string(what) + ": " + cudaGetErrorString(e);
+  return LBM_ERR_CUDA;
+}
+
+void drop_graphs(BoxState* b) {
+  for(auto& g : b->graph)
+    if(g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+}  // namespace
+
+cudaError_t box_initial_condition(BoxState* b, cudaStream_t s) {
+  // equilibrium at (init_density, init_velocity); Poisson starts from phi = 0
+  const int Q = b->Q, D = b->D;
+  double    c[19][3], w[19];
+  auto fill = [&](auto L) {
+    using LL = decltype(L);
+    for(int q = 0; q < Q; ++q) {
+      for(int d = 0; d < 3; ++d) c[q][d] = LL::c(q, d);
+      w[q] = LL::w(q);
+    }
+  };
+  if(b->desc.lattice == LBM_D2Q9) fill(Lattice<LBM_D2Q9>{});
+  else if(b->desc.lattice == LBM_D3Q19) fill(Lattice<LBM_D3Q19>{});
+  else fill(Lattice<LBM_D3Q7>{});
+  InitVec v{};
+  if(b->desc.equation == LBM_NAVIER_STOKES) {
+    const double rho = b->desc.init_density;
+    double       usq = 0;
+    for(int d = 0; d < D; ++d) usq += b->desc.init_velocity[d] * b->desc.init_velocity[d];
+    for(int q = 0; q < Q; ++q) {
+      double cu = 0;
+      for(int d = 0; d < D; ++d) cu += c[q][d] * b->desc.init_velocity[d];
+      v.f[q] = w[q] * rho * (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
+    }
+  }
+  cudaError_t e = dispatch_init(b, v, s);
+  if(e != cudaSuccess) return e;
+  b->steps     = 0;
+  b->res_ready = 0;
+  b->mom_valid = 0;
+  return cudaStreamSynchronize(s);
+}
+
+int box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
+  // All but the last two steps replay a captured one-step graph per parity.
+  // The last two record the moments (mode 1) and then the residual partials
+  // against them (mode 2), so lbm_gpu_residual is ready after any call of two
+  // or more steps; a one-step call compares with the moments the previous call
+  // left behind.
+  const int64_t plain = nsteps >= 2 ? nsteps - 2 : 0;
+  for(int64_t k = 0; k < plain; ++k) {
+    const int parity = static_cast<int>(b->steps & 1);
+    if(!b->graph[parity]) {
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      if(e != cudaSuccess) return cerr(err, e, "begin capture");
+      e              = dispatch_step(b, parity != 0, 0, s);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if(e != cudaSuccess) return cerr(err, e, "step launch");
+      if(e2 != cudaSuccess) return cerr(err, e2, "end capture");
+      e = cudaGraphInstantiate(&b->graph[parity], g, 0);
+      cudaGraphDestroy(g);
+      if(e != cudaSuccess) return cerr(err, e, "graph instantiate");
+    }
+    cudaError_t e = cudaGraphLaunch(b->graph[parity], s);
+    if(e != cudaSuccess) return cerr(err, e, "graph launch");
+    ++b->steps;
+    b->mom_valid = 0;
+    b->res_ready = 0;
+  }
+  for(int64_t k = plain; k < nsteps; ++k) {
+    const int   mom = b->mom_valid ? 2 : 1;
+    cudaError_t e   = dispatch_step(b, (b->steps & 1) != 0, mom, s);
+    if(e != cudaSuccess) return cerr(err, e, "step");
+    ++b->steps;
+    b->mom_valid = 1;
+    b->res_ready = mom == 2;
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  if(e != cudaSuccess) return cerr(err, e, "step sync");
+  return LBM_OK;
+}
+
+int box_residual(BoxState* b, double* r, cudaStream_t s, std::string& err) {
+  if(!b->res_ready) {
+    err = "residual needs a step call of at least two steps";
+    return LBM_ERR_INVALID;
+  }
+  k_final_sum<<<1, 256, 0, s>>>(b->partials, nblocks_step(b), b->nvar, b->out);
+  cudaError_t e = cudaMemcpyAsync(r, b->out, sizeof(double) * b->nvar, cudaMemcpyDeviceToHost, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if(e != cudaSuccess) return cerr(err, e, "residual");
+  for(int v = 0; v < b->nvar; ++v)
+    if(!std::isfinite(r[v])) {
+      err = "Solution diverged";
+      return LBM_ERR_DIVERGED;
+    }
+  return LBM_OK;
+}
+
+int box_get_populations(BoxState* b, double* f, cudaStream_t s, std::string& err) {
+  if(!ensure_staging(b)) {
+    err = "staging allocation failed";
+    return LBM_ERR_NOMEM;
+  }
+  cudaError_t e = dispatch_readout(b, b->f64, s);
+  if(e == cudaSuccess) e = cudaMemcpyAsync(f, b->f64, sizeof(double) * b->Q * b->p.ncells, cudaMemcpyDeviceToHost, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? LBM_OK : cerr(err, e, "get populations");
+}
+
+int box_set_populations(BoxState* b, const double* f, cudaStream_t s, std::string& err) {
+  if(!ensure_staging(b)) {
+    err = "staging allocation failed";
+    return LBM_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMemcpyAsync(b->f64, f, sizeof(double) * b->Q * b->p.ncells, cudaMemcpyHostToDevice, s);
+  if(e == cudaSuccess) e = dispatch_load(b, b->f64, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if(e != cudaSuccess) return cerr(err, e, "set populations");
+  b->steps     = 0;  // the layout is now the even-parity (standard) one
+  b->res_ready = 0;
+  b->mom_valid = 0;
+  return LBM_OK;
+}
+
+int box_mass_momentum(BoxState* b, double* out, cudaStream_t s, std::string& err) {
+  if(!ensure_staging(b)) {
+    err = "staging allocation failed";
+    return LBM_ERR_NOMEM;
+  }
+  cudaError_t e = dispatch_readout(b, b->f64, s);
+  if(e != cudaSuccess) return cerr(err, e, "readout");
+  const int nb = 304;
+  switch(b->desc.lattice) {
+    case LBM_D2Q9: k_box_sum<LBM_D2Q9><<<nb, 256, 0, s>>>(b->f64, b->p.ncells, b->partials_mm); break;
+    case LBM_D3Q19: k_box_sum<LBM_D3Q19><<<nb, 256, 0, s>>>(b->f64, b->p.ncells, b->partials_mm); break;
+    default: k_box_sum<LBM_D3Q7><<<nb, 256, 0, s>>>(b->f64, b->p.ncells, b->partials_mm); break;
+  }
+  k_final_sum<<<1, 256, 0, s>>>(b->partials_mm, nb, b->D + 1, b->out + 4);
+  e = cudaMemcpyAsync(out, b->out + 4, sizeof(double) * (b->D + 1), cudaMemcpyDeviceToHost, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? LBM_OK : cerr(err, e, "mass/momentum");
+}
+
+int box_info(const BoxState* b, int64_t* ncells, int32_t* q, int32_t* nvar) {
+  if(ncells) *ncells = b->p.ncells;
+  if(q) *q = b->Q;
+  if(nvar) *nvar = b->nvar;
+  return LBM_OK;
+}
+
+void box_destroy(BoxState* b) {
+  if(!b) return;
+  drop_graphs(b);
+  cudaFree(b->pop);
+  cudaFree(b->flags);
+  cudaFree(b->dirichlet);
+  cudaFree(b->mom);
+  cudaFree(b->partials);
+  cudaFree(b->out);
+  cudaFree(b->f64);
+  delete b;
+}
+
+// time one even+odd pair at a given block size (for the autotuner)
+float time_pair(BoxState* b, int tpb, cudaStream_t s) {
+  const int keep = b->tuned_tpb;
+  b->tuned_tpb   = tpb;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  dispatch_step(b, false, 0, s);
+  dispatch_step(b, true, 0, s);
+  cudaEventRecord(e0, s);
+  for(int k = 0; k < 2; ++k) {
+    dispatch_step(b, false, 0, s);
+    dispatch_step(b, true, 0, s);
+  }
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tuned_tpb = keep;
+  return ms;
+}
+
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" {
+
+int lbm_gpu_box_storage_bytes(int32_t storage) {
+  switch(storage) {
+    case LBM_STORE_F64: return 8;
+    case LBM_STORE_F32: return 4;
+    case LBM_STORE_F16_DEV:
+    case LBM_STORE_BF16_DEV: return 2;
+    default: return 0;
+  }
+}
+
+int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const double* dirichlet, lbm_gpu_ctx** out) {
+  if(!desc || !out) return LBM_ERR_INVALID;
+  *out = nullptr;
+  const int lat = desc->lattice, eq = desc->equation, st = desc->storage;
+  const bool ok = ((lat == LBM_D2Q9 || lat == LBM_D3Q19) && eq == LBM_NAVIER_STOKES && st >= 0 && st <= 3) ||
+                  (lat == LBM_D3Q7 && eq == LBM_POISSON && (st == LBM_STORE_F64 || st == LBM_STORE_F32));
+  if(!ok) return LBM_ERR_UNSUPPORTED;
+  const int D = lat == LBM_D2Q9 ? 2 : 3;
+  if(desc->nx < 2 || desc->ny < 2 || (D == 3 && desc->nz < 2) || (D == 2 && desc->nz != 1)) return LBM_ERR_INVALID;
+  if(desc->ny > 65535 || desc->nz > 65535) return LBM_ERR_INVALID;
+  if(!(desc->omega > 0.0 && desc->omega < 2.0)) return LBM_ERR_INVALID;
+  for(int a = 0; a < D; ++a) {
+    const bool p0 = desc->face[2 * a] == LBM_FACE_PERIODIC, p1 = desc->face[2 * a + 1] == LBM_FACE_PERIODIC;
+    if(p0 != p1) return LBM_ERR_INVALID;
+    for(int sd = 0; sd < 2; ++sd) {
+      const int ft = desc->face[2 * a + sd];
+      if(ft < 0 || ft > 3) return LBM_ERR_INVALID;
+      if(ft == LBM_FACE_OPEN && a != 0) return LBM_ERR_UNSUPPORTED;  // open faces are the x inlet / outlet planes
+    }
+  }
+  const int64_t ncells = static_cast<int64_t>(desc->nx) * desc->ny * desc->nz;
+  std::vector<uint8_t> hflags(ncells, LBM_CELL_FLUID);
+  if(flags) std::copy(flags, flags + ncells, hflags.begin());
+  bool has_outlet = false;
+  for(int64_t i = 0; i < ncells; ++i) {
+    const uint8_t t = hflags[i];
+    if(t > LBM_CELL_DIRICHLET) return LBM_ERR_INVALID;
+    const int x = static_cast<int>(i % desc->nx);
+    if(t == LBM_CELL_OUTLET) {
+      if(x != desc->nx - 1 || desc->face[1] != LBM_FACE_OPEN) return LBM_ERR_INVALID;
+      has_outlet = true;
+    }
+    if(t == LBM_CELL_DIRICHLET && (eq != LBM_POISSON || !dirichlet)) return LBM_ERR_INVALID;
+    if(t == LBM_CELL_INLET && eq != LBM_NAVIER_STOKES) return LBM_ERR_INVALID;
+    // a cell on an open face must emit (inlet) or be an outlet / solid
+    if(x == 0 && desc->face[0] == LBM_FACE_OPEN && t != LBM_CELL_INLET && t != LBM_CELL_SOLID && t != LBM_CELL_DIRICHLET) return LBM_ERR_INVALID;
+    if(x == desc->nx - 1 && desc->face[1] == LBM_FACE_OPEN && t != LBM_CELL_OUTLET && t != LBM_CELL_SOLID && t != LBM_CELL_INLET &&
+       t != LBM_CELL_DIRICHLET)
+      return LBM_ERR_INVALID;
+  }
+  if(cudaSetDevice(desc->device) != cudaSuccess) return LBM_ERR_CUDA;
+
+  BoxState* b = new(std::nothrow) BoxState();
+  if(!b) return LBM_ERR_NOMEM;
+  b->desc = *desc;
+  b->D    = D;
+  b->Q    = lat == LBM_D2Q9 ? 9 : (lat == LBM_D3Q19 ? 19 : 7);
+  b->nvar = eq == LBM_NAVIER_STOKES ? D + 1 : 1;
+  b->elem = static_cast<size_t>(lbm_gpu_box_storage_bytes(st));
+  BoxParams& p = b->p;
+  p.nx = desc->nx;
+  p.ny = desc->ny;
+  p.nz = desc->nz;
+  p.ncells = ncells;
+  // plane size rounded to 128 cells so every plane starts 256-byte aligned;
+  // the outlet ghost (Q x ny x nz values) is appended as plane Q
+  const int64_t ghost = static_cast<int64_t>(b->Q) * desc->ny * desc->nz;
+  p.nalloc = (std::max(ncells, ghost) + 127) / 128 * 128;
+  for(int i = 0; i < 6; ++i) {
+    p.face[i] = desc->face[i];
+    for(int d = 0; d < 3; ++d) p.wall_u[i][d] = desc->wall_velocity[i][d];
+  }
+  p.omega = desc->omega;
+  p.has_force = 0;
+  for(int d = 0; d < 3; ++d) {
+    p.force[d]   = desc->body_force[d];
+    p.inlet_u[d] = desc->inlet_velocity[d];
+    if(desc->body_force[d] != 0.0) p.has_force = 1;
+  }
+  p.inlet_rho  = desc->inlet_density;
+  p.kappa_sq   = desc->kappa_sq;
+  p.pb_nonlinear = desc->pb_nonlinear;
+  // D = alpha (1/2 - tau) in lattice units (src/lbm/solver.cpp:606 with dt = 1)
+  p.pb_diffusivity = Lattice<LBM_D3Q7>::poisson_alpha * (0.5 - 1.0 / desc->omega);
+  p.has_outlet = has_outlet ? 1 : 0;
+  p.mom_mode   = 0;
+
+  cudaError_t e = cudaMalloc(&b->pop, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
+  if(e == cudaSuccess) e = cudaMemset(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
+  if(e == cudaSuccess) e = cudaMalloc(&b->flags, ncells);
+  if(e == cudaSuccess) e = cudaMemcpy(b->flags, hflags.data(), ncells, cudaMemcpyHostToDevice);
+  if(e == cudaSuccess && dirichlet) {
+    e = cudaMalloc(&b->dirichlet, sizeof(double) * ncells);
+    if(e == cudaSuccess) e = cudaMemcpy(b->dirichlet, dirichlet, sizeof(double) * ncells, cudaMemcpyHostToDevice);
+  }
+  const size_t csize = st == LBM_STORE_F64 ? 8 : 4;
+  if(e == cudaSuccess) e = cudaMalloc(&b->mom, csize * b->nvar * ncells);
+  if(e == cudaSuccess) e = cudaMemset(b->mom, 0, csize * b->nvar * ncells);
+  // partials for the largest launch (smallest block size considered by the tuner)
+  const int64_t maxblocks = static_cast<int64_t>((desc->nx + 63) / 64) * desc->ny * desc->nz;
+  if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4));
+  b->partials_mm = b->partials + maxblocks * 4;
+  if(e == cudaSuccess) e = cudaMalloc(&b->out, sizeof(double) * 8);
+  if(e == cudaSuccess) {
+    k_mark_near_solid<<<static_cast<unsigned>((ncells + 255) / 256), 256>>>(b->flags, desc->nx, desc->ny, desc->nz, D);
+    e = cudaDeviceSynchronize();
+  }
+  p.flags     = b->flags;
+  p.dirichlet = b->dirichlet;
+  p.pop       = b->pop;
+  p.mom       = b->mom;
+  p.partials  = b->partials;
+  cudaStream_t stream = nullptr;
+  if(e == cudaSuccess) e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  if(e != cudaSuccess) {
+    box_destroy(b);
+    return e == cudaErrorMemoryAllocation ? LBM_ERR_NOMEM : LBM_ERR_CUDA;
+  }
+  // autotune the block size on the (not yet initialised) state
+  {
+    float best = 1e30f;
+    for(int tpb : {64, 128, 256, 512}) {
+      if(tpb > 2 * desc->nx && tpb > 64) continue;
+      const float ms = time_pair(b, tpb, stream);
+      if(ms < best) {
+        best         = ms;
+        b->tuned_tpb = tpb;
+      }
+    }
+    cudaMemsetAsync(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1), stream);
+    if(cudaStreamSynchronize(stream) != cudaSuccess) {
+      cudaStreamDestroy(stream);
+      box_destroy(b);
+      return LBM_ERR_CUDA;
+    }
+  }
+  lbm_gpu_ctx* ctx = lbm_internal_new_box_ctx(desc->device, b, stream);
+  if(!ctx) {
+    cudaStreamDestroy(stream);
+    box_destroy(b);
+    return LBM_ERR_NOMEM;
+  }
+  *out = ctx;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, double* uz) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b) return LBM_ERR_INVALID;
+  cudaStream_t s = lbm_internal_stream(ctx);
+  std::string  err;
+  if(!ensure_staging(b)) return LBM_ERR_NOMEM;
+  const int64_t N = b->p.ncells;
+  double*       d = nullptr;
+  cudaError_t   e = cudaMalloc(&d, sizeof(double) * N * 4);
+  if(e == cudaSuccess) e = dispatch_readout(b, b->f64, s);
+  if(e == cudaSuccess) {
+    const unsigned g = static_cast<unsigned>((N + 255) / 256);
+    switch(b->desc.lattice * 2 + b->desc.equation) {
+      case LBM_D2Q9 * 2: k_box_moments_f64<LBM_D2Q9, 0><<<g, 256, 0, s>>>(b->p, b->f64, d, d + N, d + 2 * N, nullptr); break;
+      case LBM_D3Q19 * 2: k_box_moments_f64<LBM_D3Q19, 0><<<g, 256, 0, s>>>(b->p, b->f64, d, d + N, d + 2 * N, d + 3 * N); break;
+      default: k_box_moments_f64<LBM_D3Q7, 1><<<g, 256, 0, s>>>(b->p, b->f64, d, nullptr, nullptr, nullptr); break;
+    }
+    e = cudaGetLastError();
+  }
+  double* outs[4] = {rho, ux, uy, uz};
+  for(int k = 0; k < 4 && e == cudaSuccess; ++k) {
+    if(!outs[k]) continue;
+    if(k > 0 && (b->desc.equation != LBM_NAVIER_STOKES || k > b->D)) continue;
+    e = cudaMemcpyAsync(outs[k], d + k * N, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  }
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  if(e != cudaSuccess) {
+    lbm_internal_set_error(ctx, std::string("box moments: ") + cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
+}
+
+int lbm_gpu_box_profile_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* total_ms, double* kernel_ms, int64_t* launches) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b || nsteps < 0) return LBM_ERR_INVALID;
+  cudaStream_t             s = lbm_internal_stream(ctx);
+  std::vector<cudaEvent_t> ev(2 * nsteps + 2);
+  for(auto& e : ev) cudaEventCreate(&e);
+  cudaEventRecord(ev[0], s);
+  cudaError_t e = cudaSuccess;
+  for(int64_t k = 0; k < nsteps && e == cudaSuccess; ++k) {
+    // same moment bookkeeping as box_step: the last two steps record the residual
+    int mom = 0;
+    if(nsteps >= 2 && k >= nsteps - 2) mom = b->mom_valid ? 2 : 1;
+    if(nsteps < 2) mom = b->mom_valid ? 2 : 1;
+    e = dispatch_step(b, (b->steps & 1) != 0, mom, s, ev[2 + 2 * k], ev[3 + 2 * k]);
+    ++b->steps;
+    b->mom_valid = mom != 0;
+    b->res_ready = mom == 2;
+  }
+  cudaEventRecord(ev[1], s);
+  if(e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+  double tot = 0, ker = 0;
+  if(e == cudaSuccess) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    tot = ms;
+    for(int64_t k = 0; k < nsteps; ++k) {
+      cudaEventElapsedTime(&ms, ev[2 + 2 * k], ev[3 + 2 * k]);
+      ker += ms;
+    }
+  }
+  for(auto& x : ev) cudaEventDestroy(x);
+  if(e != cudaSuccess) {
+    lbm_internal_set_error(ctx, std::string("profile steps: ") + cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  if(total_ms) *total_ms = tot;
+  if(kernel_ms) *kernel_ms = ker;
+  if(launches) *launches = nsteps;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b) return LBM_ERR_INVALID;
+  if(threads_per_block) *threads_per_block = b->tuned_tpb;
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// Dense-box engine: the BGK step on a structured nx*ny*nz box with a flag byte
+// per cell, AA-pattern in-place streaming and selectable population storage.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/lbm_gpu.h"
+#include "../../include/lbm_gpu_box.h"
+
+struct lbm_gpu_ctx;
+
+namespace lbm {
+
+// Everything a box kernel needs, passed by value (kernel parameter space).
+struct BoxParams {
+  int     nx, ny, nz;       // fluid box
+  int64_t ncells;           // nx*ny*nz
+  int64_t nalloc;           // cells per population plane (ncells + outlet ghost plane)
+  int     face[6];          // lbm_face per face (-x,+x,-y,+y,-z,+z)
+  double  wall_u[6][3];     // velocity of each wall face (moving bounce-back)
+  double  omega;
+  double  force[3];         // Guo body force
+  double  inlet_rho, inlet_u[3];
+  double  kappa_sq;         // Poisson-Boltzmann kappa^2
+  double  pb_diffusivity;   // alpha (1/2 - tau) in lattice units
+  int     pb_nonlinear;
+  int     has_force;
+  int     has_outlet;
+  const uint8_t* flags;     // ncells
+  const double*  dirichlet; // ncells Poisson Dirichlet values or nullptr
+  void*   pop;              // Q planes of nalloc values of the storage type
+  // residual support: moments of the previous check step (ncells x nvar, compute precision)
+  void*   mom;
+  double* partials;         // per-block partial sums of |moment change|
+  int     mom_mode;         // 0 none, 1 write moments, 2 accumulate |new-old| and write
+};
+
+struct BoxState {
+  lbm_box_desc desc;
+  BoxParams    p;
+  int          Q = 0, D = 0, nvar = 0;
+  int64_t      steps = 0;     // completed steps; parity selects the AA kernel
+  size_t       elem  = 8;     // bytes per stored population
+  void*        pop   = nullptr;
+  uint8_t*     flags = nullptr;
+  double*      dirichlet = nullptr;
+  void*        mom   = nullptr;
+  double*      partials = nullptr;     // residual partials (one per step block and variable)
+  double*      partials_mm = nullptr;  // mass / momentum partials
+  double*      out   = nullptr;
+  double*      f64   = nullptr;  // FP64 staging for transfers (Q x ncells)
+  int          nblocks_red = 0;
+  int          res_ready = 0;  // partials hold the residual of the last step
+  int          mom_valid = 0;  // mom holds the moments of the last step
+  int          tuned_tpb = 128;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
+};
+
+cudaError_t box_initial_condition(BoxState* b, cudaStream_t s);
+int         box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err);
+int         box_residual(BoxState* b, double* r, cudaStream_t s, std::string& err);
+int         box_get_populations(BoxState* b, double* f, cudaStream_t s, std::string& err);
+int         box_set_populations(BoxState* b, const double* f, cudaStream_t s, std::string& err);
+int         box_mass_momentum(BoxState* b, double* out, cudaStream_t s, std::string& err);
+int         box_info(const BoxState* b, int64_t* ncells, int32_t* q, int32_t* nvar);
+void        box_destroy(BoxState* b);
+
+}  // namespace lbm
+
+// context plumbing shared with capi.cu
+lbm_gpu_ctx*   lbm_internal_new_box_ctx(int device, lbm::BoxState* box, cudaStream_t stream);
+lbm::BoxState* lbm_internal_box(lbm_gpu_ctx* ctx);
+cudaStream_t   lbm_internal_stream(lbm_gpu_ctx* ctx);
+void           lbm_internal_set_error(lbm_gpu_ctx* ctx, const std::string& msg);

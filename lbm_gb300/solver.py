@@ -1,0 +1,360 @@
+"""Host-side mirror of the reference's LBMSolver over the GB300 C ABI.
+
+``TableSolver`` drives the reference-table engine (the solver's own cell list
+and neighbour table); ``BoxSolver`` drives the dense-box engine; ``LBMSolver``
+reproduces ``LBMSolver::run`` (src/lbm/solver.cpp:175-214) on top of a
+TableSolver: JSON constants and boundary objects, the convergence check every
+``conv_interval`` steps with the reference's residual and threshold
+(src/lbm/solver.cpp:232-263), the extra step after convergence, and the
+analytic comparison with its pass/fail bounds (src/lbm/solver.cpp:387-482).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import refconfig as rc
+from ._lib import BndDesc, BoxDesc, TableDesc, check, load
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+class TableSolver:
+    """The reference time step on the reference's own tables, on one GPU."""
+
+    def __init__(self, consts: rc.SolverConstants, grid: rc.GridTables, bnds: List[rc.BndDesc],
+                 forcing: Optional[rc.ForcingDesc] = None, device: int = 0):
+        lib = load()
+        self._lib = lib
+        self.ctx = None
+        self.n = grid.ncells
+        self.ndim = grid.ndim
+        nghbr = np.ascontiguousarray(grid.nghbr, dtype=np.int64)
+        centers = np.ascontiguousarray(grid.centers, dtype=np.float64)
+        d = TableDesc()
+        d.lattice, d.equation, d.ncells, d.nnghbr, d.device = consts.lattice, consts.equation, self.n, nghbr.shape[1], device
+        d.omega, d.relax_time, d.dt, d.poisson_k = consts.omega, consts.relax_time, consts.dt, consts.poisson_k
+        bb = np.zeros(6)
+        bb[: grid.bbox.size] = grid.bbox
+        d.bbox[:] = bb.tolist()
+        d.cell_length = grid.cell_length
+        h = C.c_void_p()
+        check(lib.lbm_gpu_create(C.byref(d), _ptr(nghbr), _ptr(centers), C.byref(h)), None, "lbm_gpu_create")
+        self.ctx = h
+        n = C.c_int64()
+        q = C.c_int32()
+        nv = C.c_int32()
+        lib.lbm_gpu_info(self.ctx, C.byref(n), C.byref(q), C.byref(nv))
+        self.q, self.nvar = q.value, nv.value
+        for b in bnds:
+            self.add_boundary(b)
+        if forcing is not None:
+            i = np.ascontiguousarray(forcing.inlet_cells, dtype=np.int64)
+            o = np.ascontiguousarray(forcing.outlet_cells, dtype=np.int64)
+            check(lib.lbm_gpu_set_forcing(self.ctx, forcing.pressure_gradient, i.size, _ptr(i), o.size, _ptr(o)), self.ctx,
+                  "set_forcing")
+
+    def add_boundary(self, b: rc.BndDesc):
+        cells = np.ascontiguousarray(b.cells, dtype=np.int64)
+        normals = np.ascontiguousarray(b.normals, dtype=np.float64)
+        values = None if b.values is None else np.ascontiguousarray(b.values, dtype=np.float64)
+        conn = None if b.conn_cells is None else np.ascontiguousarray(b.conn_cells, dtype=np.int64)
+        connn = None if b.conn_normals is None else np.ascontiguousarray(b.conn_normals, dtype=np.float64)
+        d = BndDesc()
+        d.kind, d.has_vec, d.has_pressure = b.kind, int(b.has_vec), int(b.has_pressure)
+        d.ncells, d.cells, d.normals, d.values = cells.size, _ptr(cells), _ptr(normals), _ptr(values)
+        d.vec[:] = [float(x) for x in np.asarray(b.vec, dtype=np.float64)[:3]]
+        d.scalar = float(b.scalar)
+        d.nconn = 0 if conn is None else conn.size
+        d.conn_cells, d.conn_normals = _ptr(conn), _ptr(connn)
+        check(self._lib.lbm_gpu_add_boundary(self.ctx, C.byref(d)), self.ctx, f"add_boundary {b.name}")
+
+    def close(self):
+        if self.ctx:
+            self._lib.lbm_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initial_condition(self):
+        check(self._lib.lbm_gpu_initial_condition(self.ctx), self.ctx, "initial_condition")
+
+    def step(self, n: int = 1):
+        check(self._lib.lbm_gpu_step(self.ctx, int(n)), self.ctx, "step")
+
+    def residual(self) -> np.ndarray:
+        r = np.zeros(self.nvar)
+        check(self._lib.lbm_gpu_residual(self.ctx, _ptr(r)), self.ctx, "residual")
+        return r
+
+    def residual_unchecked(self) -> np.ndarray:
+        """The residual even when it is NaN/Inf (the caller decides on divergence)."""
+        r = np.zeros(self.nvar)
+        rc_ = self._lib.lbm_gpu_residual(self.ctx, _ptr(r))
+        if rc_ not in (0, -5):
+            check(rc_, self.ctx, "residual")
+        return r
+
+    def update_moments(self):
+        check(self._lib.lbm_gpu_update_moments(self.ctx), self.ctx, "update_moments")
+
+    def vars(self) -> np.ndarray:
+        v = np.zeros(self.n * self.nvar)
+        check(self._lib.lbm_gpu_get_vars(self.ctx, _ptr(v)), self.ctx, "get_vars")
+        return v
+
+    def varsold(self) -> np.ndarray:
+        v = np.zeros(self.n * self.nvar)
+        check(self._lib.lbm_gpu_get_varsold(self.ctx, _ptr(v)), self.ctx, "get_varsold")
+        return v
+
+    def set_vars(self, v: np.ndarray):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        check(self._lib.lbm_gpu_set_vars(self.ctx, _ptr(v)), self.ctx, "set_vars")
+
+    def populations(self) -> np.ndarray:
+        f = np.zeros(self.n * self.q)
+        check(self._lib.lbm_gpu_get_populations(self.ctx, _ptr(f)), self.ctx, "get_populations")
+        return f
+
+    def set_populations(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        check(self._lib.lbm_gpu_set_populations(self.ctx, _ptr(f)), self.ctx, "set_populations")
+
+    def mass_momentum(self) -> np.ndarray:
+        out = np.zeros(1 + self.ndim)
+        check(self._lib.lbm_gpu_reduce_mass_momentum(self.ctx, _ptr(out)), self.ctx, "mass_momentum")
+        return out
+
+
+FACE = {"wall": 0, "periodic": 1, "freeslip": 2, "open": 3}
+STORAGE = {"f64": 0, "f32": 1, "f16dev": 2, "bf16dev": 3}
+STORAGE_BYTES = {0: 8, 1: 4, 2: 2, 3: 2}
+
+
+class BoxSolver:
+    """The step on a dense box (nx, ny, nz) with a flag byte per cell."""
+
+    def __init__(self, lattice: int, shape, omega: float, storage: str = "f64", faces=("wall",) * 6, flags=None,
+                 wall_velocity=None, body_force=(0, 0, 0), inlet_velocity=(0, 0, 0), inlet_density=1.0,
+                 init_density=1.0, init_velocity=(0, 0, 0), equation: int = rc.EQ_NAVIER_STOKES, kappa_sq: float = 0.0,
+                 pb_nonlinear: bool = True, dirichlet=None, device: int = 0):
+        lib = load()
+        self._lib = lib
+        self.ctx = None
+        nx, ny, nz = (tuple(shape) + (1, 1))[:3]
+        self.shape = (nx, ny, nz)
+        self.ncells = nx * ny * nz
+        self.lattice = lattice
+        self.q = rc.LATTICE_Q[lattice]
+        self.ndim = rc.LATTICE_DIM[lattice]
+        self.equation = equation
+        d = BoxDesc()
+        d.lattice, d.equation, d.storage, d.device = lattice, equation, STORAGE[storage], device
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.face[:] = [FACE[f] if isinstance(f, str) else int(f) for f in faces]
+        d.omega = omega
+        wv = np.zeros((6, 3)) if wall_velocity is None else np.asarray(wall_velocity, dtype=np.float64).reshape(6, 3)
+        for i in range(6):
+            d.wall_velocity[i][:] = wv[i].tolist()
+        d.body_force[:] = [float(x) for x in body_force]
+        d.inlet_density = inlet_density
+        d.inlet_velocity[:] = [float(x) for x in inlet_velocity]
+        d.init_density = init_density
+        d.init_velocity[:] = [float(x) for x in init_velocity]
+        d.kappa_sq = kappa_sq
+        d.pb_nonlinear = int(pb_nonlinear)
+        self.storage = STORAGE[storage]
+        fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        di = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.float64).reshape(-1)
+        h = C.c_void_p()
+        check(lib.lbm_gpu_create_box(C.byref(d), _ptr(fl), _ptr(di), C.byref(h)), None, "lbm_gpu_create_box")
+        self.ctx = h
+        self.nvar = 1 if equation == rc.EQ_POISSON else self.ndim + 1
+
+    def close(self):
+        if self.ctx:
+            self._lib.lbm_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initial_condition(self):
+        check(self._lib.lbm_gpu_initial_condition(self.ctx), self.ctx, "initial_condition")
+
+    def step(self, n: int = 1):
+        check(self._lib.lbm_gpu_step(self.ctx, int(n)), self.ctx, "step")
+
+    def synchronize(self):
+        check(self._lib.lbm_gpu_synchronize(self.ctx), self.ctx, "synchronize")
+
+    def residual(self) -> np.ndarray:
+        r = np.zeros(self.nvar)
+        check(self._lib.lbm_gpu_residual(self.ctx, _ptr(r)), self.ctx, "residual")
+        return r
+
+    def populations(self) -> np.ndarray:
+        f = np.zeros(self.q * self.ncells)
+        check(self._lib.lbm_gpu_get_populations(self.ctx, _ptr(f)), self.ctx, "get_populations")
+        return f.reshape(self.q, self.ncells)
+
+    def set_populations(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        check(self._lib.lbm_gpu_set_populations(self.ctx, _ptr(f)), self.ctx, "set_populations")
+
+    def moments(self):
+        n = self.ncells
+        rho = np.zeros(n)
+        u = [np.zeros(n) for _ in range(3)]
+        check(self._lib.lbm_gpu_box_moments(self.ctx, _ptr(rho), _ptr(u[0]), _ptr(u[1]), _ptr(u[2])), self.ctx, "moments")
+        return rho, np.stack(u[: self.ndim]) if self.equation == rc.EQ_NAVIER_STOKES else None
+
+    def mass_momentum(self) -> np.ndarray:
+        out = np.zeros(1 + self.ndim)
+        check(self._lib.lbm_gpu_reduce_mass_momentum(self.ctx, _ptr(out)), self.ctx, "mass_momentum")
+        return out
+
+    def profile_steps(self, n: int):
+        """Run n steps with a CUDA event pair around every step-kernel launch;
+        returns (device ms of the whole sequence, summed kernel ms, launches)."""
+        tot, ker, cnt = C.c_double(), C.c_double(), C.c_int64()
+        check(self._lib.lbm_gpu_box_profile_steps(self.ctx, int(n), C.byref(tot), C.byref(ker), C.byref(cnt)), self.ctx,
+              "profile_steps")
+        return tot.value, ker.value, cnt.value
+
+    def threads_per_block(self) -> int:
+        t = C.c_int32()
+        check(self._lib.lbm_gpu_box_autotune(self.ctx, C.byref(t)), self.ctx, "autotune")
+        return t.value
+
+
+# ---- the reference's run loop -------------------------------------------------
+
+def analytical_solution(name: str, ndim: int, nu: float, dp: float):
+    """The reference's analytic solutions (src/lbm/analytical_solutions.h:15-101)."""
+    if name == "couette2D_1_5":
+        relax, re, h = 0.9, 0.75, 5.0
+        refv = re * (2.0 * relax - 1.0) / 6.0 / 1.0
+        return lambda x: np.array([refv / h * x[1], 0.0])
+    if name == "poiseuille2D_1":
+        return lambda x: np.array([dp / (2.0 * nu) * x[1] * (1 - 0 - x[1]), 0.0])
+    if name == "poissonCHAI08_1":
+        k = 27.79
+        epk, emk = math.exp(k), math.exp(-k)
+        return lambda x: np.array([(epk - 1.0) / (epk - emk) * math.exp(-k * x[0]) + (1.0 - emk) / (epk - emk) * math.exp(k * x[0])])
+    if name == "poissonCHAI08_2":
+        mu = math.sqrt(4 + math.pi * math.pi)
+        return lambda x: np.array([math.cos(math.pi * x[0]) * math.sinh(mu * (1 - x[1])) / math.sinh(mu), 0.0])
+    if name == "poissonSimpleDiffReaction":
+        th = 1.0
+        return lambda x: np.array([math.cosh(th * (1.0 - x[0])) / math.cosh(th)])
+    raise rc.ConfigError("Invalid analyticalSolution :" + name + " selected!")
+
+
+class LBMSolver:
+    """``LBMSolver::run`` over the GPU step (same keys, same loop, same checks)."""
+
+    def __init__(self, solver_cfg: dict, grid: rc.GridTables, device: int = 0):
+        self.cfg = solver_cfg
+        self.grid = grid
+        self.consts = rc.solver_constants(solver_cfg, grid)
+        self.bnds = rc.boundary_list(solver_cfg, grid, self.consts)
+        self.forcing = rc.forcing_desc(solver_cfg, grid)
+        self.gpu = TableSolver(self.consts, grid, self.bnds, self.forcing, device=device)
+        self.steps_done = 0
+        self.converged = False
+        self.diverged = False
+
+    def run(self, max_steps: Optional[int] = None) -> Dict:
+        """The iteration loop of ``LBMSolver::run``: at iteration t the convergence
+        check (every conv_interval, decisive from t > 1), then the time step, then
+        the output, which recomputes the moments every solution_interval steps, at
+        the last step and on convergence.  Steps between two such events run as
+        one batched call."""
+        cfg = self.cfg
+        max_steps = int(cfg["maxSteps"]) if max_steps is None else max_steps
+        ci = int(cfg.get("conv_interval", cfg.get("info_interval", 10)))
+        si = int(cfg.get("solution_interval", 100))
+        crit = float(cfg.get("convergence", 1e-12))
+        g = self.gpu
+        g.initial_condition()
+        t = 0
+        last_res = None
+        while t < max_steps:
+            conv = False
+            if t > 0 and t % ci == 0:
+                res = g.residual_unchecked()
+                last_res = res
+                m = float(np.max(res))
+                if t > 1 and m < crit:
+                    conv = True
+                if t > 1 and not math.isfinite(m):
+                    self.diverged = True
+                    conv = True
+            g.step(1)
+            if (t > 0 and t % si == 0) or t == max_steps - 1 or conv:
+                g.update_moments()
+            t += 1
+            if conv:
+                self.converged = not self.diverged
+                break
+            # next iteration with an event: a check before it or an output after it
+            nxt = t
+            while nxt < max_steps - 1 and not ((nxt > 0 and nxt % ci == 0) or (nxt > 0 and nxt % si == 0)):
+                nxt += 1
+            if nxt > t:
+                g.step(nxt - t)
+                t = nxt
+        self.steps_done = t
+        return {"steps": t, "converged": self.converged, "diverged": self.diverged,
+                "residual": None if last_res is None else last_res.tolist()}
+
+    def compare_to_analytical(self) -> Dict:
+        """``compareToAnalyticalResult`` (src/lbm/solver.cpp:387-482)."""
+        cfg, grid = self.cfg, self.grid
+        name = cfg["analyticalSolution"]
+        dp = float(cfg["poiseuillePressureGradient"]) if name == "poiseuille2D_1" else 0.0
+        sol = analytical_solution(name, grid.ndim, self.consts.nu, dp)
+        excluded = set()
+        for sname in cfg.get("analyticalSolutionExcludeSurface", []):
+            excluded.update(int(c) for c in grid.surfaces[sname]["cells"])
+        v = self.gpu.vars().reshape(grid.ncells, self.consts.nvar)
+        n = grid.ncells
+        s_err = s_err2 = s_sol = s_sol2 = 0.0
+        max_err = 0.0
+        for cell in range(n):
+            if cell in excluded:
+                continue
+            x = grid.centers[cell].copy()
+            if name == "poissonCHAI08_1":
+                ext = abs(grid.centers[0, 0] - grid.centers[n - 1, 0])
+                pos = math.floor(x[0] / (ext / (n - 1)))
+                x[0] = pos * 1.0 / (n - 1)
+            s = sol(x)
+            val = v[cell, : grid.ndim] if self.consts.equation == rc.EQ_NAVIER_STOKES else np.array([v[cell, 0]] + [0.0] * (s.size - 1))
+            delta = float(np.linalg.norm(val - s))
+            s_err += delta
+            s_err2 += delta ** 2
+            s_sol += float(np.linalg.norm(s))
+            s_sol2 += float(np.dot(s, s))
+            max_err = max(max_err, delta)
+        l2 = (math.sqrt(s_err2) / math.sqrt(s_sol2)) / math.pow(n, 1.0 / grid.ndim)
+        gre = s_err / s_sol
+        bounds = {"errorMax": float(cfg.get("errorMax", 1.0)), "errorL2": float(cfg.get("errorL2", 1.0)),
+                  "errorGRE": float(cfg.get("errorGRE", 1.0))}
+        passed = not (bounds["errorMax"] < max_err or bounds["errorL2"] < l2 or math.isnan(l2) or bounds["errorGRE"] < gre
+                      or math.isnan(gre))
+        return {"max": max_err, "l2": l2, "gre": gre, "bounds": bounds, "passed": passed}

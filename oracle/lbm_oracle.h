@@ -87,13 +87,12 @@ enum { ORA_CELL_FLUID = 0, ORA_CELL_SOLID = 1, ORA_CELL_INLET = 2, ORA_CELL_OUTL
 typedef struct ora_box ora_box;
 
 /* Dense box nx*ny*nz (nz=1, ny=1 for lower dimensions), x fastest.
- * periodic[3]: wrap in that axis; walls on non-periodic faces are halfway
- * bounce-back unless freeslip[axis] is set, in which case they reflect
- * specularly.  flags may be NULL (all fluid).  lid_velocity moves the +y face
- * (2D) with a tangential x velocity.  body_force is applied with Guo's scheme. */
-ora_box* ora_box_create(int lattice, int equation, int nx, int ny, int nz, double omega, const uint8_t* flags, const int* periodic,
-                        const int* freeslip, const double* body_force, const double* inlet_velocity, double inlet_density,
-                        double lid_velocity);
+ * face[6]: treatment of the -x,+x,-y,+y,-z,+z faces (wall, periodic, free
+ * slip, open; the values of include/lbm_gpu_box.h), wall_u: 6x3 wall
+ * velocities, flags: per-cell flag bytes (NULL = all fluid), body_force:
+ * Guo forcing. */
+ora_box* ora_box_create(int lattice, int equation, int nx, int ny, int nz, double omega, const uint8_t* flags, const int* face,
+                        const double* wall_u, const double* body_force, const double* inlet_velocity, double inlet_density);
 void ora_box_destroy(ora_box* b);
 /* Poisson-Boltzmann: phi_dirichlet per cell for CELL_DIRICHLET cells,
  * kappa^2 and the sinh nonlinearity switch. */

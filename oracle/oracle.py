@@ -59,7 +59,7 @@ def lib():
         L.ora_ndist.argtypes = [vp]
         L.ora_ndist.restype = i32
         L.ora_box_create.restype = vp
-        L.ora_box_create.argtypes = [i32, i32, i32, i32, i32, dbl, vp, vp, vp, vp, vp, dbl, dbl]
+        L.ora_box_create.argtypes = [i32, i32, i32, i32, i32, dbl, vp, vp, vp, vp, vp, dbl]
         L.ora_box_destroy.argtypes = [vp]
         L.ora_box_set_poisson.argtypes = [vp, dbl, i32, vp]
         L.ora_box_set_poisson.restype = i32
@@ -135,3 +135,61 @@ class TableOracle:
         vo = np.zeros(self.n * self.nvar)
         lib().ora_get(self.h, _p(fold), _p(f), _p(v), _p(vo))
         return fold, f, v, vo
+
+
+class BoxOracle:
+    """Dense-box engine of the oracle (same arguments as the GPU BoxSolver)."""
+
+    FACE = {"wall": 0, "periodic": 1, "freeslip": 2, "open": 3}
+
+    def __init__(self, lattice, shape, omega, faces=("wall",) * 6, flags=None, wall_velocity=None, body_force=(0, 0, 0),
+                 inlet_velocity=(0, 0, 0), inlet_density=1.0, equation=0, kappa_sq=0.0, pb_nonlinear=True, dirichlet=None):
+        L = lib()
+        nx, ny, nz = (tuple(shape) + (1, 1))[:3]
+        self.shape = (nx, ny, nz)
+        self.ncells = nx * ny * nz
+        self.q = {0: 3, 1: 5, 2: 9, 3: 7, 4: 19}[lattice]
+        self.ndim = 2 if lattice == 2 else 3
+        self.equation = equation
+        face = np.array([self.FACE[f] if isinstance(f, str) else int(f) for f in faces], dtype=np.int32)
+        wv = np.zeros((6, 3)) if wall_velocity is None else np.asarray(wall_velocity, dtype=np.float64).reshape(6, 3)
+        fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        bf = np.asarray(body_force, dtype=np.float64)
+        iv = np.asarray(inlet_velocity, dtype=np.float64)
+        wv = np.ascontiguousarray(wv)
+        self._keep = [face, wv, fl, bf, iv]
+        self.h = L.ora_box_create(lattice, equation, nx, ny, nz, omega, _p(fl), _p(face), _p(wv), _p(bf), _p(iv),
+                                  inlet_density)
+        if not self.h:
+            raise ValueError("oracle: unsupported box")
+        if equation == 1:
+            di = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.float64).reshape(-1)
+            self._keep.append(di)
+            L.ora_box_set_poisson(self.h, kappa_sq, int(pb_nonlinear), _p(di))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_box_destroy(self.h)
+            self.h = None
+
+    def init_equilibrium(self, rho=1.0, u=(0, 0, 0)):
+        uu = np.asarray(u, dtype=np.float64)
+        lib().ora_box_init_equilibrium(self.h, rho, _p(uu))
+
+    def step(self, n, threads=1):
+        lib().ora_box_step(self.h, int(n), int(threads))
+
+    def populations(self):
+        f = np.zeros(self.q * self.ncells)
+        lib().ora_box_get(self.h, _p(f), None, None)
+        return f.reshape(self.q, self.ncells)
+
+    def set_populations(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        lib().ora_box_set(self.h, _p(f))
+
+    def moments(self):
+        rho = np.zeros(self.ncells)
+        u = np.zeros(3 * self.ncells)
+        lib().ora_box_get(self.h, None, _p(rho), _p(u))
+        return rho, u.reshape(3, self.ncells)[: self.ndim]

@@ -1,0 +1,164 @@
+"""Dense-box engine (AA in-place streaming) against the oracle and the reference.
+
+* FP64 box vs the reference's own solver on the Couette fixtures (moving
+  bounce-back lid, periodic x): relative L2 <= 1e-12.
+* FP64 box vs the oracle's two-array box engine on cases that exercise every
+  box feature: D3Q19 with a solid sphere, free-slip side walls, equilibrium
+  inlet and zero-gradient outlet; Guo forcing; moving lids; D3Q7
+  Poisson-Boltzmann.  Both step parities of the AA pattern are read out.
+* Reduced-precision storage against FP64 within per-format bounds.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import box_index, load_case, rel_l2
+from lbm_gb300 import refconfig as rc
+from lbm_gb300.solver import BoxSolver
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def sphere_flags(shape, center, radius, inlet_outlet=True):
+    nx, ny, nz = shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    r2 = (x + 0.5 - center[0]) ** 2 + (y + 0.5 - center[1]) ** 2 + (z + 0.5 - center[2]) ** 2
+    fl = np.zeros((nz, ny, nx), dtype=np.uint8)
+    fl[r2 < radius * radius] = 1
+    if inlet_outlet:
+        fl[:, :, 0] = 2
+        fl[:, :, -1] = 3
+    return fl.reshape(-1)
+
+
+@pytest.mark.parametrize("name", ["couette_1", "couette_50"])
+def test_box_fp64_matches_reference_couette(name):
+    meta, solver, grid, out, consts, bnds, forcing = load_case(name)
+    ij, (nx, ny) = box_index(grid)
+    tv = [b for b in bnds if b.kind == rc.BND_WALL_BB_TANGENTIAL][0].scalar
+    wv = np.zeros((6, 3))
+    wv[3, 0] = tv
+    g = BoxSolver(rc.LATTICES["D2Q9"], (nx, ny, 1), consts.omega, "f64", faces=("periodic", "periodic", "wall", "wall", "wall", "wall"),
+                  wall_velocity=wv)
+    g.initial_condition()
+    g.step(meta["steps"])
+    f = g.populations()  # (9, nx*ny), x fastest
+    idx = ij[:, 0] + nx * ij[:, 1]
+    ref = out["fold"].reshape(grid.ncells, 9)
+    assert rel_l2(f[:, idx].T, ref) <= TOL
+
+
+CASES = {
+    "d3q19_sphere_open": dict(lattice=4, shape=(24, 14, 12), omega=1 / 0.56, faces=("open", "open", "freeslip", "freeslip", "freeslip", "freeslip"),
+                              sphere=((8.0, 7.0, 6.0), 3.2), inlet=(0.05, 0, 0)),
+    "d3q19_guo_walls": dict(lattice=4, shape=(12, 10, 9), omega=1 / 0.8, faces=("periodic", "periodic", "wall", "wall", "freeslip", "freeslip"),
+                            sphere=((6.0, 5.0, 4.5), 2.5), force=(1e-5, 0, 0)),
+    "d3q19_lid": dict(lattice=4, shape=(10, 9, 8), omega=1 / 0.7, faces=("wall",) * 6, lid=(3, (0.05, 0.0, 0.02))),
+    "d2q9_guo_channel": dict(lattice=2, shape=(16, 10, 1), omega=1 / 0.8, faces=("periodic", "periodic", "wall", "wall", "wall", "wall"),
+                             force=(1e-6, 0, 0)),
+    "d2q9_cavity": dict(lattice=2, shape=(12, 12, 1), omega=1 / 0.6, faces=("wall",) * 6, lid=(3, (0.1, 0.0, 0.0))),
+    "d2q9_open_cylinder": dict(lattice=2, shape=(30, 12, 1), omega=1 / 0.6, faces=("open", "open", "freeslip", "wall", "wall", "wall"),
+                               sphere=((9.0, 6.0, 0.5), 2.6), inlet=(0.04, 0, 0)),
+}
+
+
+def make_pair(case, storage="f64"):
+    c = CASES[case]
+    shape = c["shape"]
+    flags = None
+    if "sphere" in c:
+        flags = sphere_flags(shape, c["sphere"][0], c["sphere"][1], inlet_outlet=c["faces"][0] == "open")
+    wv = np.zeros((6, 3))
+    if "lid" in c:
+        wv[c["lid"][0]] = c["lid"][1]
+    kw = dict(faces=c["faces"], flags=flags, wall_velocity=wv, body_force=c.get("force", (0, 0, 0)),
+              inlet_velocity=c.get("inlet", (0, 0, 0)))
+    g = BoxSolver(c["lattice"], shape, c["omega"], storage, **kw)
+    o = oracle.BoxOracle(c["lattice"], shape, c["omega"], **kw)
+    return g, o
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("steps", [1, 2, 37, 60])
+def test_box_fp64_matches_oracle(case, steps):
+    g, o = make_pair(case)
+    g.initial_condition()
+    o.init_equilibrium(1.0, (0, 0, 0))
+    g.step(steps)
+    o.step(steps)
+    assert rel_l2(g.populations(), o.populations()) <= TOL
+
+
+@pytest.mark.parametrize("case", ["d3q19_sphere_open", "d2q9_guo_channel"])
+def test_set_populations_round_trip(case):
+    g, o = make_pair(case)
+    g.initial_condition()
+    g.step(5)
+    f = g.populations()
+    o.set_populations(f)
+    g.set_populations(f)
+    assert np.array_equal(g.populations(), f)
+    g.step(9)
+    o.step(9)
+    assert rel_l2(g.populations(), o.populations()) <= TOL
+
+
+@pytest.mark.parametrize("storage,bound", [("f32", 1e-5), ("f16dev", 5e-3), ("bf16dev", 5e-2)])
+def test_reduced_precision_storage_against_fp64(storage, bound):
+    ref, _ = make_pair("d3q19_sphere_open", "f64")
+    low, _ = make_pair("d3q19_sphere_open", storage)
+    for s in (ref, low):
+        s.initial_condition()
+        s.step(300)
+    _, u64 = ref.moments()
+    _, ulo = low.moments()
+    err = rel_l2(ulo, u64)
+    print(f"{storage}: velocity relative L2 vs FP64 after 300 steps = {err:.3e}")
+    assert err <= bound
+
+
+def test_mass_conservation_closed_box():
+    g, _ = make_pair("d3q19_lid")
+    g.initial_condition()
+    m0 = g.mass_momentum()[0]
+    g.step(200)
+    m1 = g.mass_momentum()[0]
+    assert abs(m1 - m0) / m0 < 1e-12
+
+
+def test_residual_matches_moment_change():
+    g, o = make_pair("d2q9_cavity")
+    g.initial_condition()
+    g.step(10)
+    r1 = g.residual()
+    rho_a, u_a = g.moments()
+    g.step(1)
+    rho_b, u_b = g.moments()
+    r = g.residual()
+    # the residual of the last step is sum |moments(t) - moments(t-1)|
+    expect = [np.abs(rho_b - rho_a).sum()] + [np.abs(u_b[d] - u_a[d]).sum() for d in range(2)]
+    assert np.allclose(r, expect, rtol=1e-9, atol=1e-15), (r, expect)
+    assert np.all(np.isfinite(r1))
+
+
+def test_poisson_boltzmann_d3q7_matches_oracle():
+    shape = (14, 12, 10)
+    nx, ny, nz = shape
+    flags = np.zeros((nz, ny, nx), dtype=np.uint8)
+    phi = np.zeros((nz, ny, nx))
+    flags[0, :, :] = flags[-1, :, :] = 4
+    flags[:, 0, :] = flags[:, -1, :] = 4
+    flags[:, :, 0] = flags[:, :, -1] = 4
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ball = (x - 7) ** 2 + (y - 6) ** 2 + (z - 5) ** 2 < 9
+    flags[ball] = 4
+    phi[ball] = 2.0
+    kw = dict(faces=("wall",) * 6, flags=flags.reshape(-1), equation=1, kappa_sq=1.0 / 16, pb_nonlinear=True, dirichlet=phi.reshape(-1))
+    g = BoxSolver(rc.LATTICES["D3Q7"], shape, 1.0, "f64", **kw)
+    o = oracle.BoxOracle(rc.LATTICES["D3Q7"], shape, 1.0, **kw)
+    g.initial_condition()
+    o.init_equilibrium()
+    g.step(41)
+    o.step(41)
+    assert rel_l2(g.populations(), o.populations()) <= TOL
