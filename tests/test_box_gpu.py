@@ -128,18 +128,21 @@ def test_mass_conservation_closed_box():
 
 
 def test_residual_matches_moment_change():
+    """The residual after step t is sum |m(t-1) - m(t-2)| over cells, m(k) the
+    moments of the state after k steps: the step kernel sees the moments of its
+    input, exactly like the reference's vars/varsold pair (solver.cpp:505-553)."""
     g, o = make_pair("d2q9_cavity")
     g.initial_condition()
-    g.step(10)
-    r1 = g.residual()
+    g.step(9)
     rho_a, u_a = g.moments()
     g.step(1)
     rho_b, u_b = g.moments()
+    g.step(1)
     r = g.residual()
-    # the residual of the last step is sum |moments(t) - moments(t-1)|
     expect = [np.abs(rho_b - rho_a).sum()] + [np.abs(u_b[d] - u_a[d]).sum() for d in range(2)]
     assert np.allclose(r, expect, rtol=1e-9, atol=1e-15), (r, expect)
-    assert np.all(np.isfinite(r1))
+    g.step(2)
+    assert np.all(np.isfinite(g.residual()))
 
 
 def test_poisson_boltzmann_d3q7_matches_oracle():
