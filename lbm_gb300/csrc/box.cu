@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "box.h"
@@ -169,86 +170,96 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
   return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
 }
 
+// ---- compile-time loops over the directions ------------------------------
+// Every per-direction statement of the step is instantiated with a constant q,
+// so lattice velocities, weights and plane offsets fold into immediates and
+// the populations stay in registers.
+template <class F, int... Is>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
 // ---- collision -------------------------------------------------------------
 // f (or its deviation from w for DEV storage) in, post-collision out
 template <int LAT, int EQ, class C, bool DEV>
-__device__ __forceinline__ void collide(const BoxParams& P, C* f, int64_t cell, C* mom_out) {
+__device__ __forceinline__ void collide(const BoxParams& P, C* f, C* mom_out) {
   using L         = Lattice<LAT>;
   constexpr int Q = L::Q, D = L::D;
   const C       omega = static_cast<C>(P.omega);
   if constexpr(EQ == LBM_NAVIER_STOKES) {
     C rho0 = 0, j[3] = {0, 0, 0};
-#pragma unroll
-    for(int q = 0; q < Q; ++q) {
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
       rho0 += f[q];
-#pragma unroll
-      for(int d = 0; d < D; ++d) {
-        if(L::c(q, d) > 0) j[d] += f[q];
-        if(L::c(q, d) < 0) j[d] -= f[q];
-      }
-    }
+      static_for<D>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        if constexpr(L::c(q, d) > 0) j[d] += f[q];
+        if constexpr(L::c(q, d) < 0) j[d] -= f[q];
+      });
+    });
     // DEV: rho0 is rho - 1 (sum of deviations), j is exact since sum c w = 0
     const C rho  = DEV ? C(1) + rho0 : rho0;
     const C irho = C(1) / rho;
     C       u[3] = {0, 0, 0};
     C       F[3] = {0, 0, 0};
-    if(P.has_force) {
-#pragma unroll
-      for(int d = 0; d < D; ++d) F[d] = static_cast<C>(P.force[d]);
+    const bool force = P.has_force != 0;
+    if(force) {
+      static_for<D>([&](auto dc) { F[decltype(dc)::value] = static_cast<C>(P.force[decltype(dc)::value]); });
     }
-#pragma unroll
-    for(int d = 0; d < D; ++d) u[d] = (j[d] + C(0.5) * F[d]) * irho;
+    static_for<D>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      u[d]            = (j[d] + C(0.5) * F[d]) * irho;
+    });
     C usq = 0;
-#pragma unroll
-    for(int d = 0; d < D; ++d) usq += u[d] * u[d];
+    static_for<D>([&](auto dc) { usq += u[decltype(dc)::value] * u[decltype(dc)::value]; });
     if(mom_out) {
       mom_out[0] = rho;
-#pragma unroll
-      for(int d = 0; d < D; ++d) mom_out[1 + d] = u[d];
+      static_for<D>([&](auto dc) { mom_out[1 + decltype(dc)::value] = u[decltype(dc)::value]; });
     }
     const C guo = C(1) - C(0.5) * omega;
-#pragma unroll
-    for(int q = 0; q < Q; ++q) {
-      C cu = 0;
-#pragma unroll
-      for(int d = 0; d < D; ++d) {
-        if(L::c(q, d) > 0) cu += u[d];
-        if(L::c(q, d) < 0) cu -= u[d];
-      }
-      const C w = static_cast<C>(L::w(q));
-      // feq - w = w (rho - 1 + rho (3 cu + 4.5 cu^2 - 1.5 u^2)) for DEV storage
-      const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
-      C       feq;
-      if(DEV) feq = w * (rho0 + rho * poly);
-      else feq = w * rho * (C(1) + poly);
-      C out = f[q] + omega * (feq - f[q]);
-      if(P.has_force) {
+    // feq - w = w (rho - 1 + rho (3 cu + 4.5 cu^2 - 1.5 u^2)) for DEV storage
+    const C k0 = DEV ? rho0 - rho * C(1.5) * usq : rho * (C(1) - C(1.5) * usq);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      C             cu = 0;
+      static_for<D>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        if constexpr(L::c(q, d) > 0) cu += u[d];
+        if constexpr(L::c(q, d) < 0) cu -= u[d];
+      });
+      constexpr C w   = static_cast<C>(L::w(q));
+      const C     feq = w * (k0 + rho * cu * (C(3) + C(4.5) * cu));
+      C           out = f[q] + omega * (feq - f[q]);
+      if(force) {
         C cf = 0, uf = 0;
-#pragma unroll
-        for(int d = 0; d < D; ++d) {
+        static_for<D>([&](auto dc) {
+          constexpr int d = decltype(dc)::value;
           cf += static_cast<C>(L::c(q, d)) * F[d];
           uf += u[d] * F[d];
-        }
+        });
         out += guo * w * (C(3) * (cf - uf) + C(9) * cu * cf);
       }
       f[q] = out;
-    }
+    });
   } else {
     // Poisson(-Boltzmann), Chai & Shi: phi from the moving populations
     C acc = 0;
-#pragma unroll
-    for(int q = 0; q < Q - 1; ++q) acc += f[q];
+    static_for<Q - 1>([&](auto qc) { acc += f[decltype(qc)::value]; });
     const C phi = acc * static_cast<C>(1.0 / (1.0 - L::w(Q - 1)));
     if(mom_out) mom_out[0] = phi;
     const C g   = P.pb_nonlinear ? static_cast<C>(sinh(static_cast<double>(phi))) : phi;
     const C src = static_cast<C>(P.pb_diffusivity * P.kappa_sq) * g;
-#pragma unroll
-    for(int q = 0; q < Q; ++q) {
-      const C feq = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
-      C       out = f[q] + omega * (feq - f[q]);
-      if(q != Q - 1) out += static_cast<C>(L::pw(q)) * src;
+    static_for<Q>([&](auto qc) {
+      constexpr int q   = decltype(qc)::value;
+      const C       feq = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+      C             out = f[q] + omega * (feq - f[q]);
+      if constexpr(q != Q - 1) out += static_cast<C>(L::pw(q)) * src;
       f[q] = out;
-    }
+    });
   }
 }
 
@@ -260,21 +271,24 @@ __device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* f, int64
   if constexpr(EQ == LBM_NAVIER_STOKES) {
     const C rho = static_cast<C>(P.inlet_rho);
     C       usq = 0;
-#pragma unroll
-    for(int d = 0; d < D; ++d) usq += static_cast<C>(P.inlet_u[d] * P.inlet_u[d]);
-#pragma unroll
-    for(int q = 0; q < Q; ++q) {
-      C cu = 0;
-#pragma unroll
-      for(int d = 0; d < D; ++d) cu += static_cast<C>(L::c(q, d)) * static_cast<C>(P.inlet_u[d]);
+    static_for<D>([&](auto dc) { usq += static_cast<C>(P.inlet_u[decltype(dc)::value] * P.inlet_u[decltype(dc)::value]); });
+    static_for<Q>([&](auto qc) {
+      constexpr int q  = decltype(qc)::value;
+      C             cu = 0;
+      static_for<D>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        cu += static_cast<C>(L::c(q, d)) * static_cast<C>(P.inlet_u[d]);
+      });
       const C w    = static_cast<C>(L::w(q));
       const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
       f[q]         = DEV ? w * ((rho - C(1)) + rho * poly) : w * rho * (C(1) + poly);
-    }
+    });
   } else {
     const C phi = P.dirichlet ? static_cast<C>(P.dirichlet[cell]) : C(0);
-#pragma unroll
-    for(int q = 0; q < Q; ++q) f[q] = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      f[q]            = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+    });
   }
 }
 
@@ -284,119 +298,182 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// ---- the step kernel ---------------------------------------------------------
+// block sum of the per-thread residual contributions into partials[k*stride + slot]
+template <int NV>
+__device__ __forceinline__ void block_partials(const double* diff, double* partials, int64_t stride, int64_t slot) {
+  __shared__ double red[NV][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for(int k = 0; k < NV; ++k) {
+    const double s = warp_sum(diff[k]);
+    if(lane == 0) red[k][wid] = s;
+  }
+  __syncthreads();
+  if(wid == 0) {
+#pragma unroll
+    for(int k = 0; k < NV; ++k) {
+      double s = lane < nw ? red[k][lane] : 0.0;
+      s        = warp_sum(s);
+      if(lane == 0) partials[k * stride + slot] = s;
+    }
+  }
+}
+
+template <int LAT, int EQ, class C, int MOM, int NV>
+__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, double* diff) {
+  if constexpr(MOM != 0) {
+    C* M = static_cast<C*>(P.mom);
+#pragma unroll
+    for(int k = 0; k < NV; ++k) {
+      if constexpr(MOM == 2) diff[k] = fabs(static_cast<double>(mom[k]) - static_cast<double>(M[k * P.ncells + cell]));
+      M[k * P.ncells + cell] = mom[k];
+    }
+  }
+}
+
+// ---- the step kernels ----------------------------------------------------------
+// k_box_bulk: 3D grid over the box, one thread per cell.
+//   even step: every non-solid cell; reads and writes only its own slots.
+//   odd step:  cells whose links all stay inside the box and avoid solids;
+//              pull from x - c_q, push to x + c_q with constant offsets.
+// k_box_bnd: odd step only, the remaining cells (next to a face or a solid,
+//   inlet / outlet / Dirichlet planes) from a compact list; every link is
+//   resolved through the faces.  Each population slot is read and then
+//   written by the one thread that owns it, so the two kernels may run in
+//   either order.
 // MOM: 0 plain, 1 also write the moments, 2 also accumulate |moments - previous|
 template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__global__ void __launch_bounds__(512) k_box_step(BoxParams P) {
+__global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
   using C         = typename S::C;
-  constexpr int Q = L::Q, D = L::D;
+  constexpr int Q = L::Q;
   constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
-  constexpr int NV   = EQ == LBM_NAVIER_STOKES ? D + 1 : 1;
+  constexpr int NV   = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
 
   const int  x     = blockIdx.x * blockDim.x + threadIdx.x;
   const int  y     = blockIdx.y;
   const int  z     = blockIdx.z;
   const bool valid = x < P.nx;
-  const int64_t cell = valid ? x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z) : 0;
+  const int  cell  = valid ? x + P.nx * (y + P.ny * z) : 0;
   const uint8_t flag = valid ? P.flags[cell] : LBM_CELL_SOLID;
   const uint8_t type = flag & TYPE_MASK;
   T*            A    = static_cast<T*>(P.pop);
-  const int64_t NA   = P.nalloc;
+  const int     NA   = static_cast<int>(P.nalloc);
   double        diff[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) diff[k] = 0.0;
 
-  if(type != LBM_CELL_SOLID) {
+  bool work;
+  if constexpr(ODD) work = type == LBM_CELL_FLUID && !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+  else work = type != LBM_CELL_SOLID;
+
+  if(work) {
     C f[Q];
     C mom[NV];
-    if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
+#pragma unroll
+    for(int k = 0; k < NV; ++k) mom[k] = 0;
+    const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+    if(emit) {
       emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
-#pragma unroll
-      for(int k = 0; k < NV; ++k) mom[k] = 0;
     } else {
-      const bool fast = !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
-      if(!ODD) {
-#pragma unroll
-        for(int q = 0; q < Q; ++q) f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q)));
+      if constexpr(!ODD) {
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          f[q]            = S::load(A[q * NA + cell], static_cast<C>(L::w(q)));
+        });
         if(type == LBM_CELL_OUTLET) {
-          // links from beyond +x: what the upstream cell received (ghost)
-#pragma unroll
-          for(int q = 0; q < Q; ++q)
-            if(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
+          // links from beyond +x: what the upstream cell received (ghost plane)
+          static_for<Q>([&](auto qc) {
+            constexpr int q = decltype(qc)::value;
+            if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], static_cast<C>(L::w(q)));
+          });
         }
-      } else if(fast) {
-#pragma unroll
-        for(int q = 0; q < Q; ++q) f[q] = S::load(A[L::opp(q) * NA + cell - offset<LAT>(P, q)], static_cast<C>(L::w(q)));
       } else {
-#pragma unroll
-        for(int q = 0; q < Q; ++q) {
-          const Link lk = resolve<LAT>(P, x, y, z, q, -1, q);
-          if(lk.kind == LINK_CELL) {
-            f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], static_cast<C>(L::w(q)));
-          } else if(lk.kind == LINK_BOUNCE) {
-            f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr);
-          } else {
-            f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
-          }
-        }
+        const int sy = P.nx, sz = P.nx * P.ny;
+        static_for<Q>([&](auto qc) {
+          constexpr int q   = decltype(qc)::value;
+          const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+          f[q]              = S::load(A[L::opp(q) * NA + cell - off], static_cast<C>(L::w(q)));
+        });
       }
-      collide<LAT, EQ, C, DEV>(P, f, cell, MOM ? mom : nullptr);
+      collide<LAT, EQ, C, DEV>(P, f, MOM ? mom : nullptr);
     }
-    if constexpr(MOM != 0) {
-      C* M = static_cast<C*>(P.mom);
-#pragma unroll
-      for(int k = 0; k < NV; ++k) {
-        if(MOM == 2) diff[k] = fabs(static_cast<double>(mom[k]) - static_cast<double>(M[k * P.ncells + cell]));
-        M[k * P.ncells + cell] = mom[k];
-      }
-    }
-    // write back
-    if(!ODD) {
-#pragma unroll
-      for(int q = 0; q < Q; ++q) A[L::opp(q) * NA + cell] = S::store(f[q], static_cast<C>(L::w(L::opp(q))));
+    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
+    if constexpr(!ODD) {
+      static_for<Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        A[L::opp(q) * NA + cell] = S::store(f[q], static_cast<C>(L::w(L::opp(q))));
+      });
     } else {
-      const bool fast = !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
-      if(fast) {
-#pragma unroll
-        for(int q = 0; q < Q; ++q) A[q * NA + cell + offset<LAT>(P, q)] = S::store(f[q], static_cast<C>(L::w(q)));
-      } else {
-#pragma unroll
-        for(int q = 0; q < Q; ++q) {
-          const Link lk = resolve<LAT>(P, x, y, z, q, +1, L::opp(q));
-          if(lk.kind == LINK_CELL) {
-            A[lk.q * NA + lk.cell] = S::store(f[q], static_cast<C>(L::w(lk.q)));
-          } else if(lk.kind == LINK_BOUNCE) {
-            const int o       = L::opp(q);
-            A[o * NA + cell] = S::store(f[q] + static_cast<C>(lk.corr), static_cast<C>(L::w(o)));
-          }
-          // LINK_OPEN: the population leaves the box
-        }
-      }
+      const int sy = P.nx, sz = P.nx * P.ny;
+      static_for<Q>([&](auto qc) {
+        constexpr int q   = decltype(qc)::value;
+        const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+        A[q * NA + cell + off] = S::store(f[q], static_cast<C>(L::w(q)));
+      });
     }
   }
   if constexpr(MOM == 2) {
-    __shared__ double red[NV][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for(int k = 0; k < NV; ++k) {
-      const double s = warp_sum(diff[k]);
-      if(lane == 0) red[k][wid] = s;
-    }
-    __syncthreads();
-    if(wid == 0) {
-      const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
-      const int64_t nb = static_cast<int64_t>(gridDim.x) * gridDim.y * gridDim.z;
-#pragma unroll
-      for(int k = 0; k < NV; ++k) {
-        double s = lane < nw ? red[k][lane] : 0.0;
-        s        = warp_sum(s);
-        if(lane == 0) P.partials[k * nb + b] = s;
-      }
-    }
+    const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
+    block_partials<NV>(diff, P.partials, P.partial_stride, b);
   }
+}
+
+template <int LAT, int EQ, int ST, int MOM>
+__global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int n, int64_t slot0) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
+  constexpr int NV   = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
+  const int     i    = blockIdx.x * blockDim.x + threadIdx.x;
+  double        diff[NV];
+#pragma unroll
+  for(int k = 0; k < NV; ++k) diff[k] = 0.0;
+  if(i < n) {
+    const int     cell = list[i];
+    const int     x = cell % P.nx, y = (cell / P.nx) % P.ny, z = cell / (P.nx * P.ny);
+    const uint8_t type = P.flags[cell] & TYPE_MASK;
+    T*            A    = static_cast<T*>(P.pop);
+    const int64_t NA   = P.nalloc;
+    C             f[Q];
+    C             mom[NV];
+#pragma unroll
+    for(int k = 0; k < NV; ++k) mom[k] = 0;
+    if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
+      emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+    } else {
+      static_for<Q>([&](auto qc) {
+        constexpr int q  = decltype(qc)::value;
+        const Link    lk = resolve<LAT>(P, x, y, z, q, -1, q);
+        if(lk.kind == LINK_CELL) {
+          f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], static_cast<C>(L::w(q)));
+        } else if(lk.kind == LINK_BOUNCE) {
+          f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr);
+        } else {
+          f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
+        }
+      });
+      collide<LAT, EQ, C, DEV>(P, f, MOM ? mom : nullptr);
+    }
+    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
+    static_for<Q>([&](auto qc) {
+      constexpr int q  = decltype(qc)::value;
+      const Link    lk = resolve<LAT>(P, x, y, z, q, +1, L::opp(q));
+      if(lk.kind == LINK_CELL) {
+        A[lk.q * NA + lk.cell] = S::store(f[q], static_cast<C>(L::w(lk.q)));
+      } else if(lk.kind == LINK_BOUNCE) {
+        constexpr int o   = L::opp(q);
+        A[o * NA + cell] = S::store(f[q] + static_cast<C>(lk.corr), static_cast<C>(L::w(o)));
+      }
+      // LINK_OPEN: the population leaves the box
+    });
+  }
+  if constexpr(MOM == 2) block_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x);
 }
 
 // outlet ghost fill, run before every step: for each outlet cell and each
@@ -554,22 +631,6 @@ __global__ void k_box_moments_f64(BoxParams P, const double* f, double* rho, dou
   }
 }
 
-__global__ void k_mark_near_solid(uint8_t* flags, int nx, int ny, int nz, int dims) {
-  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  const int64_t n    = static_cast<int64_t>(nx) * ny * nz;
-  if(cell >= n) return;
-  const int x = static_cast<int>(cell % nx), y = static_cast<int>((cell / nx) % ny), z = static_cast<int>(cell / (static_cast<int64_t>(nx) * ny));
-  bool near = false;
-  for(int dz = (dims > 2 ? -1 : 0); dz <= (dims > 2 ? 1 : 0); ++dz)
-    for(int dy = (dims > 1 ? -1 : 0); dy <= (dims > 1 ? 1 : 0); ++dy)
-      for(int dx = -1; dx <= 1; ++dx) {
-        const int xx = x + dx, yy = y + dy, zz = z + dz;
-        if(xx < 0 || yy < 0 || zz < 0 || xx >= nx || yy >= ny || zz >= nz) continue;
-        if((flags[xx + static_cast<int64_t>(nx) * (yy + static_cast<int64_t>(ny) * zz)] & TYPE_MASK) == LBM_CELL_SOLID) near = true;
-      }
-  flags[cell] = static_cast<uint8_t>((flags[cell] & TYPE_MASK) | (near ? NEAR_SOLID : 0));
-}
-
 // sum over cells of the FP64 populations: mass and momentum
 template <int LAT>
 __global__ void k_box_sum(const double* f, int64_t n, double* partials) {
@@ -605,11 +666,11 @@ __global__ void k_box_sum(const double* f, int64_t n, double* partials) {
   }
 }
 
-__global__ void k_final_sum(const double* partials, int64_t nb, int nvec, double* out) {
+__global__ void k_final_sum(const double* partials, int64_t nb, int64_t stride, int nvec, double* out) {
   __shared__ double sh[32];
   for(int v = 0; v < nvec; ++v) {
     double acc = 0;
-    for(int64_t i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[v * nb + i];
+    for(int64_t i = threadIdx.x; i < nb; i += blockDim.x) acc += partials[v * stride + i];
     acc = warp_sum(acc);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if(lane == 0) sh[wid] = acc;
@@ -638,14 +699,23 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p);
   }
   if(ev0) cudaEventRecord(ev0, s);
+  const int64_t nbulk = static_cast<int64_t>(g.x) * g.y * g.z;
+  const unsigned nbb  = static_cast<unsigned>((b->n_bnd + 127) / 128);
   if(odd) {
-    if(mom == 0) k_box_step<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
-    else if(mom == 1) k_box_step<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
-    else k_box_step<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
+    if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
+    else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
+    else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
+    if(nbb) {
+      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
+      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
+      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
+    }
+    if(mom == 2) b->res_slots = nbulk + nbb;
   } else {
-    if(mom == 0) k_box_step<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
-    else if(mom == 1) k_box_step<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
-    else k_box_step<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
+    if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
+    else if(mom == 1) k_box_bulk<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
+    else k_box_bulk<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
+    if(mom == 2) b->res_slots = nbulk;
   }
   if(ev1) cudaEventRecord(ev1, s);
   return cudaGetLastError();
@@ -696,10 +766,6 @@ cudaError_t launch_init(BoxState* b, const InitVec& v, cudaStream_t s) {
 }
 cudaError_t dispatch_init(BoxState* b, const InitVec& v, cudaStream_t s) { LBM_BOX_DISPATCH(launch_init, b, v, s); }
 
-int64_t nblocks_step(const BoxState* b) {
-  const dim3 g = step_grid(b, b->tuned_tpb);
-  return static_cast<int64_t>(g.x) * g.y * g.z;
-}
 
 bool ensure_staging(BoxState* b) {
   if(b->f64) return true;
@@ -799,7 +865,7 @@ int box_residual(BoxState* b, double* r, cudaStream_t s, std::string& err) {
     err = "residual needs a step call of at least two steps";
     return LBM_ERR_INVALID;
   }
-  k_final_sum<<<1, 256, 0, s>>>(b->partials, nblocks_step(b), b->nvar, b->out);
+  k_final_sum<<<1, 256, 0, s>>>(b->partials, b->res_slots, b->p.partial_stride, b->nvar, b->out);
   cudaError_t e = cudaMemcpyAsync(r, b->out, sizeof(double) * b->nvar, cudaMemcpyDeviceToHost, s);
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return cerr(err, e, "residual");
@@ -850,7 +916,7 @@ int box_mass_momentum(BoxState* b, double* out, cudaStream_t s, std::string& err
     case LBM_D3Q19: k_box_sum<LBM_D3Q19><<<nb, 256, 0, s>>>(b->f64, b->p.ncells, b->partials_mm); break;
     default: k_box_sum<LBM_D3Q7><<<nb, 256, 0, s>>>(b->f64, b->p.ncells, b->partials_mm); break;
   }
-  k_final_sum<<<1, 256, 0, s>>>(b->partials_mm, nb, b->D + 1, b->out + 4);
+  k_final_sum<<<1, 256, 0, s>>>(b->partials_mm, nb, nb, b->D + 1, b->out + 4);
   e = cudaMemcpyAsync(out, b->out + 4, sizeof(double) * (b->D + 1), cudaMemcpyDeviceToHost, s);
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? LBM_OK : cerr(err, e, "mass/momentum");
@@ -873,6 +939,7 @@ void box_destroy(BoxState* b) {
   cudaFree(b->partials);
   cudaFree(b->out);
   cudaFree(b->f64);
+  cudaFree(b->bnd_list);
   delete b;
 }
 
@@ -974,6 +1041,10 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   // the outlet ghost (Q x ny x nz values) is appended as plane Q
   const int64_t ghost = static_cast<int64_t>(b->Q) * desc->ny * desc->nz;
   p.nalloc = (std::max(ncells, ghost) + 127) / 128 * 128;
+  if(p.nalloc * (b->Q + 1) >= (int64_t(1) << 31)) {
+    delete b;
+    return LBM_ERR_UNSUPPORTED;  // the step kernels index populations with 32-bit offsets
+  }
   for(int i = 0; i < 6; ++i) {
     p.face[i] = desc->face[i];
     for(int d = 0; d < 3; ++d) p.wall_u[i][d] = desc->wall_velocity[i][d];
@@ -995,6 +1066,32 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
 
   cudaError_t e = cudaMalloc(&b->pop, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
   if(e == cudaSuccess) e = cudaMemset(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
+  // engine bit: a stencil neighbour is solid; and the compact list of cells the
+  // odd step must resolve link by link (next to a face or a solid, or not fluid)
+  {
+    const int nx = desc->nx, ny = desc->ny, nz = desc->nz;
+    std::vector<int32_t> list;
+    for(int64_t i = 0; i < ncells; ++i) {
+      const int x = static_cast<int>(i % nx), y = static_cast<int>((i / nx) % ny), z = static_cast<int>(i / (static_cast<int64_t>(nx) * ny));
+      if(hflags[i] == LBM_CELL_SOLID) continue;
+      bool near = false;
+      for(int dz = (D > 2 ? -1 : 0); dz <= (D > 2 ? 1 : 0) && !near; ++dz)
+        for(int dy = -1; dy <= 1 && !near; ++dy)
+          for(int dx = -1; dx <= 1 && !near; ++dx) {
+            if(std::abs(dx) + std::abs(dy) + std::abs(dz) > (lat == LBM_D3Q7 ? 1 : 2)) continue;
+            const int xx = x + dx, yy = y + dy, zz = z + dz;
+            if(xx < 0 || yy < 0 || zz < 0 || xx >= nx || yy >= ny || zz >= nz) continue;
+            if(hflags[xx + static_cast<int64_t>(nx) * (yy + static_cast<int64_t>(ny) * zz)] == LBM_CELL_SOLID) near = true;
+          }
+      const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && (D < 3 || (z > 0 && z < nz - 1));
+      if(near || !inside || hflags[i] != LBM_CELL_FLUID) list.push_back(static_cast<int32_t>(i));
+      if(near) hflags[i] = static_cast<uint8_t>(hflags[i] | NEAR_SOLID);
+    }
+    b->n_bnd = static_cast<int64_t>(list.size());
+    if(e == cudaSuccess) e = cudaMalloc(&b->bnd_list, sizeof(int32_t) * std::max<size_t>(1, list.size()));
+    if(e == cudaSuccess && !list.empty())
+      e = cudaMemcpy(b->bnd_list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice);
+  }
   if(e == cudaSuccess) e = cudaMalloc(&b->flags, ncells);
   if(e == cudaSuccess) e = cudaMemcpy(b->flags, hflags.data(), ncells, cudaMemcpyHostToDevice);
   if(e == cudaSuccess && dirichlet) {
@@ -1005,14 +1102,11 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   if(e == cudaSuccess) e = cudaMalloc(&b->mom, csize * b->nvar * ncells);
   if(e == cudaSuccess) e = cudaMemset(b->mom, 0, csize * b->nvar * ncells);
   // partials for the largest launch (smallest block size considered by the tuner)
-  const int64_t maxblocks = static_cast<int64_t>((desc->nx + 63) / 64) * desc->ny * desc->nz;
+  const int64_t maxblocks = static_cast<int64_t>((desc->nx + 63) / 64) * desc->ny * desc->nz + (b->n_bnd + 127) / 128;
   if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4));
-  b->partials_mm = b->partials + maxblocks * 4;
+  b->partials_mm      = b->partials + maxblocks * 4;
+  p.partial_stride    = maxblocks;
   if(e == cudaSuccess) e = cudaMalloc(&b->out, sizeof(double) * 8);
-  if(e == cudaSuccess) {
-    k_mark_near_solid<<<static_cast<unsigned>((ncells + 255) / 256), 256>>>(b->flags, desc->nx, desc->ny, desc->nz, D);
-    e = cudaDeviceSynchronize();
-  }
   p.flags     = b->flags;
   p.dirichlet = b->dirichlet;
   p.pop       = b->pop;
@@ -1027,7 +1121,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   // autotune the block size on the (not yet initialised) state
   {
     float best = 1e30f;
-    for(int tpb : {64, 128, 256, 512}) {
+    for(int tpb : {64, 128, 256}) {
       if(tpb > 2 * desc->nx && tpb > 64) continue;
       const float ms = time_pair(b, tpb, stream);
       if(ms < best) {

@@ -35,6 +35,7 @@ struct BoxParams {
   // residual support: moments of the previous check step (ncells x nvar, compute precision)
   void*   mom;
   double* partials;         // per-block partial sums of |moment change|
+  int64_t partial_stride;   // slots per variable in partials
   int     mom_mode;         // 0 none, 1 write moments, 2 accumulate |new-old| and write
 };
 
@@ -52,10 +53,12 @@ struct BoxState {
   double*      partials_mm = nullptr;  // mass / momentum partials
   double*      out   = nullptr;
   double*      f64   = nullptr;  // FP64 staging for transfers (Q x ncells)
-  int          nblocks_red = 0;
   int          res_ready = 0;  // partials hold the residual of the last step
   int          mom_valid = 0;  // mom holds the moments of the last step
   int          tuned_tpb = 128;
+  int32_t*     bnd_list  = nullptr;  // cells the odd step resolves link by link
+  int64_t      n_bnd     = 0;
+  int64_t      res_slots = 0;        // partial slots written by the last residual step
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
 };
 
