@@ -138,6 +138,24 @@ int lbm_gpu_info(const lbm_gpu_ctx* ctx, int64_t* ncells, int32_t* q, int32_t* n
 const char* lbm_gpu_last_error(const lbm_gpu_ctx* ctx);
 void        lbm_gpu_destroy(lbm_gpu_ctx* ctx);
 
+/* Residual without any device allocation.  No counterpart in the reference:
+ * it serves callers that cannot call cudaMalloc -- code whose device memory
+ * belongs to another allocator (a framework's caching allocator, a fixed
+ * arena) and latency-critical code that cannot afford cudaMalloc's implicit
+ * synchronisation.  It computes out[v] = sum_i |vars[v*ncells+i] -
+ * varsold[v*ncells+i]| for v < nvar (the reference's sumAbsDiff,
+ * src/lbm/solver.cpp:808-815) on caller-owned DEVICE arrays, variable-major,
+ * writing nvar doubles to the DEVICE array `out`, asynchronously on `stream`
+ * (a cudaStream_t; NULL = legacy default stream) of the current device.
+ * Scratch: a fixed array in the library's device image (304 x
+ * LBM_GPU_NOALLOC_MAX_VARS doubles per GPU, kept until the process exits),
+ * shared by every call: calls that overlap on the GPU race.  nvar above
+ * LBM_GPU_NOALLOC_MAX_VARS is rejected with LBM_ERR_INVALID.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture. */
+#define LBM_GPU_NOALLOC_MAX_VARS 8
+int lbm_gpu_residual_noalloc(const double* vars, const double* varsold, int64_t ncells, int32_t nvar, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

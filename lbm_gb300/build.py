@@ -28,6 +28,7 @@ UNITS = {
     "reduce.cu": [],
     "box.cu": [],
     "capi.cu": [],
+    "noalloc.cu": [],
 }
 
 
