@@ -156,7 +156,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
+    ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
+                    help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
     args = ap.parse_args()
+    if args.profile_case:
+        from lbm_gb300.solver import BoxSolver
+
+        case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
+        s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
+                      inlet_velocity=case["inlet"])
+        s.initial_condition()
+        s.step(4)
+        s.synchronize()
+        print(json.dumps({"profile_case": args.profile_case, "threads_per_block": s.threads_per_block()}))
+        return
     if args.warmup < 3:
         args.warmup = 3
 
