@@ -32,10 +32,12 @@ extern "C" {
 
 /* population storage */
 typedef enum lbm_storage {
-  LBM_STORE_F64     = 0, /* FP64 populations, FP64 arithmetic (the plain method) */
-  LBM_STORE_F32     = 1, /* FP32 populations, FP32 arithmetic */
-  LBM_STORE_F16_DEV = 2, /* FP16 of (f_i - w_i) / w_i * 2^12, FP32 arithmetic */
-  LBM_STORE_BF16_DEV = 3 /* BF16 of the same scaled deviation, FP32 arithmetic */
+  /* Navier-Stokes populations are held as the scaled deviation
+   * (f_i - w_i) / w_i * 2^12 in every storage; Poisson populations as f_i */
+  LBM_STORE_F64     = 0, /* FP64 storage, FP64 arithmetic (the plain method) */
+  LBM_STORE_F32     = 1, /* FP32 storage, FP32 arithmetic */
+  LBM_STORE_F16_DEV = 2, /* FP16 storage, FP32 arithmetic */
+  LBM_STORE_BF16_DEV = 3 /* BF16 storage, FP32 arithmetic */
 } lbm_storage;
 
 /* treatment of a face of the box */
@@ -91,6 +93,44 @@ int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
  * device time of the whole sequence, kernel_ms the summed duration of the
  * step-kernel launches, launches their count (any pointer may be NULL). */
 int lbm_gpu_box_profile_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* total_ms, double* kernel_ms, int64_t* launches);
+
+/* ---- batched cavities --------------------------------------------------
+ * Many independent D2Q9 lid-driven cavities (n x n, halfway bounce-back on
+ * every wall, the +y wall moving in x at lid_velocity) advance together in one
+ * persistent launch per step.  Used for parameter sweeps (Reynolds number,
+ * size) that the reference runs one case at a time.  lbm_gpu_step,
+ * lbm_gpu_initial_condition (rest equilibrium), lbm_gpu_info and
+ * lbm_gpu_destroy apply to the returned context. */
+typedef struct lbm_batch_desc {
+  int32_t lattice;  /* LBM_D2Q9 */
+  int32_t storage;  /* lbm_storage */
+  int32_t device;
+  int32_t ndomains;
+  double  lid_velocity;
+} lbm_batch_desc;
+
+int lbm_gpu_create_batch(const lbm_batch_desc* desc, const int32_t* sides, const double* omegas, lbm_gpu_ctx** out);
+/* res[d*3 + v]: residual (rho, ux, uy) of every cavity after the last step
+ * call of at least two steps (cavities no longer active keep their last value) */
+int lbm_gpu_batch_residuals(lbm_gpu_ctx* ctx, double* res);
+/* Step all active cavities, checking every check_interval steps; a cavity
+ * whose largest residual drops below tol stops.  steps_done[d]: steps taken.
+ * A cavity whose residual is NaN/Inf stops too; the call then finishes the
+ * others and returns LBM_ERR_DIVERGED, naming it in lbm_gpu_last_error. */
+int lbm_gpu_batch_run(lbm_gpu_ctx* ctx, int64_t max_steps, int64_t check_interval, double tol, int64_t* steps_done);
+/* per-cavity state after lbm_gpu_batch_run (reset by lbm_gpu_initial_condition) */
+typedef enum lbm_batch_status {
+  LBM_BATCH_ACTIVE    = 0, /* still stepping */
+  LBM_BATCH_CONVERGED = 1, /* residual fell below the tolerance */
+  LBM_BATCH_DIVERGED  = 2  /* residual became NaN/Inf */
+} lbm_batch_status;
+int lbm_gpu_batch_status(lbm_gpu_ctx* ctx, int32_t* status);
+/* FP64 post-stream populations of cavity d, f[q * n*n + x + n*y] */
+int lbm_gpu_batch_get_domain(lbm_gpu_ctx* ctx, int32_t d, double* f);
+/* as lbm_gpu_box_profile_steps, for the batched step kernel */
+int lbm_gpu_batch_profile_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* total_ms, double* kernel_ms, int64_t* launches);
+/* the launch shape the autotuner chose */
+int lbm_gpu_batch_tuning(lbm_gpu_ctx* ctx, int32_t* grid, int32_t* threads_per_block);
 
 /* Bytes of one population in the chosen storage. */
 int lbm_gpu_box_storage_bytes(int32_t storage);

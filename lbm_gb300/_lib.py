@@ -44,6 +44,11 @@ class BoxDesc(C.Structure):
                 ("kappa_sq", C.c_double), ("pb_nonlinear", C.c_int32), ("reserved", C.c_int32)]
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("lattice", C.c_int32), ("storage", C.c_int32), ("device", C.c_int32), ("ndomains", C.c_int32),
+                ("lid_velocity", C.c_double)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -71,6 +76,14 @@ _SIGS = {
     "lbm_gpu_box_moments": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "lbm_gpu_box_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "lbm_gpu_box_storage_bytes": (C.c_int, [C.c_int32]),
+    "lbm_gpu_create_batch": (C.c_int, [C.POINTER(BatchDesc), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "lbm_gpu_batch_residuals": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_gpu_batch_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_double, C.c_void_p]),
+    "lbm_gpu_batch_get_domain": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "lbm_gpu_batch_status": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_gpu_batch_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_int64)]),
+    "lbm_gpu_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lbm_gpu_residual_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
     "lbm_gpu_box_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int64)]),

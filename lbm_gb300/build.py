@@ -29,6 +29,7 @@ UNITS = {
     "box.cu": [],
     "capi.cu": [],
     "noalloc.cu": [],
+    "batch.cu": [],
 }
 
 

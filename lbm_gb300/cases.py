@@ -1,0 +1,101 @@
+"""Seeded synthetic inputs for the benchmark configurations.
+
+No dataset is involved: every domain is generated from its description and a
+seed, with the shapes, sizes and value ranges of the workloads the project is
+measured on.
+
+* :func:`poiseuille_guo`   D2Q9 channel 256 x 64, halfway bounce-back walls,
+  periodic in x, Guo body force g, tau 0.8 (plain FP64 method).
+* :func:`sphere_channel`   D3Q19 512 x 256 x 256 flow past a sphere of radius
+  24 voxelised on cell centres, equilibrium inlet u = 0.05, zero-gradient
+  outlet, free-slip side walls, tau drawn from [0.52, 0.6].
+* :func:`pb_spheres`       D3Q7 Poisson-Boltzmann on 256^3: 1-64 charged
+  non-overlapping spheres of radius 4-16 with surface potential in [0.5, 4]
+  (units of kT/e), Debye length in [4, 32] cells, phi = 0 on the box.
+* :func:`cavities`         the batched lid-driven cavities: sides in
+  [32, 512], Re log-uniform in [10, 1000], lid velocity 0.1.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List
+
+import numpy as np
+
+D2Q9, D3Q7, D3Q19 = 2, 3, 4
+FLUID, SOLID, INLET, OUTLET, DIRICHLET = 0, 1, 2, 3, 4
+
+
+def poiseuille_guo(nx: int = 256, ny: int = 64, tau: float = 0.8, g: float = 1e-6) -> Dict:
+    """Body-force driven channel: walls (halfway bounce-back) at y = -1/2 and
+    y = ny - 1/2 in cell-centre coordinates, so the exact steady profile is
+    u(y) = g / (2 nu) s (ny - s) with s = y + 1/2 and nu = (tau - 1/2)/3."""
+    return dict(lattice=D2Q9, shape=(nx, ny, 1), omega=1.0 / tau, faces=("periodic", "periodic", "wall", "wall", "wall", "wall"),
+                body_force=(g, 0.0, 0.0), tau=tau, g=g)
+
+
+def poiseuille_profile(ny: int, tau: float, g: float) -> np.ndarray:
+    nu = (tau - 0.5) / 3.0
+    s = np.arange(ny) + 0.5
+    return g / (2.0 * nu) * s * (ny - s)
+
+
+def sphere_channel(nx=512, ny=256, nz=256, radius=24.0, center=(128.0, 128.0, 128.0), seed=2026, u_in=0.05) -> Dict:
+    rng = np.random.default_rng(seed)
+    tau = float(rng.uniform(0.52, 0.6))
+    flags = np.zeros((nz, ny, nx), dtype=np.uint8)
+    lo = [max(0, int(math.floor(c - radius - 1))) for c in center]
+    hi = [int(math.ceil(c + radius + 1)) for c in center]
+    z, y, x = np.meshgrid(np.arange(lo[2], min(hi[2], nz)), np.arange(lo[1], min(hi[1], ny)), np.arange(lo[0], min(hi[0], nx)),
+                          indexing="ij")
+    inside = (x + 0.5 - center[0]) ** 2 + (y + 0.5 - center[1]) ** 2 + (z + 0.5 - center[2]) ** 2 < radius * radius
+    flags[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]][inside] = SOLID
+    flags[:, :, 0] = INLET
+    flags[:, :, -1] = OUTLET
+    return dict(lattice=D3Q19, shape=(nx, ny, nz), omega=1.0 / tau, tau=tau, flags=flags.reshape(-1),
+                faces=("open", "open", "freeslip", "freeslip", "freeslip", "freeslip"), inlet_velocity=(u_in, 0.0, 0.0))
+
+
+def pb_spheres(n: int = 256, seed: int = 7, count: int | None = None, tau: float = 1.0) -> Dict:
+    """Charged spheres in an electrolyte: cells inside a sphere carry the
+    sphere's potential, the outermost layer of the box carries 0, everything
+    else relaxes to nabla^2 phi = kappa^2 sinh(phi)."""
+    rng = np.random.default_rng(seed)
+    count = int(rng.integers(1, 65)) if count is None else count
+    debye = float(rng.uniform(4.0, 32.0))
+    spheres: List = []
+    tries = 0
+    while len(spheres) < count and tries < 100000:
+        tries += 1
+        r = float(rng.uniform(4.0, 16.0))
+        c = rng.uniform(r + 2, n - r - 2, size=3)
+        if all(np.linalg.norm(c - c2) > r + r2 + 2 for c2, r2, _ in spheres):
+            spheres.append((c, r, float(rng.uniform(0.5, 4.0))))
+    flags = np.zeros((n, n, n), dtype=np.uint8)
+    phi = np.zeros((n, n, n))
+    for c, r, ps in spheres:
+        lo = [max(0, int(math.floor(v - r - 1))) for v in c]
+        hi = [min(n, int(math.ceil(v + r + 1))) for v in c]
+        z, y, x = np.meshgrid(np.arange(lo[2], hi[2]), np.arange(lo[1], hi[1]), np.arange(lo[0], hi[0]), indexing="ij")
+        m = (x + 0.5 - c[0]) ** 2 + (y + 0.5 - c[1]) ** 2 + (z + 0.5 - c[2]) ** 2 < r * r
+        flags[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]][m] = DIRICHLET
+        phi[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]][m] = ps
+    for sl in (np.s_[0, :, :], np.s_[-1, :, :], np.s_[:, 0, :], np.s_[:, -1, :], np.s_[:, :, 0], np.s_[:, :, -1]):
+        flags[sl] = DIRICHLET
+        phi[sl] = 0.0
+    return dict(lattice=D3Q7, shape=(n, n, n), omega=1.0 / tau, equation=1, kappa_sq=1.0 / debye ** 2, flags=flags.reshape(-1),
+                dirichlet=phi.reshape(-1), faces=("wall",) * 6, spheres=spheres, debye=debye)
+
+
+def cavities(count: int = 2048, seed: int = 11, lid: float = 0.1, nmin: int = 32, nmax: int = 512) -> Dict:
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(nmin, nmax + 1, size=count)
+    re = np.exp(rng.uniform(math.log(10.0), math.log(1000.0), size=count))
+    tau = 3.0 * lid * sides / re + 0.5
+    return dict(sides=sides.astype(np.int32), re=re, tau=tau, lid=lid)
+
+
+def box_kwargs(case: Dict) -> Dict:
+    """The BoxSolver / BoxOracle keyword arguments of a case."""
+    keys = ("faces", "flags", "wall_velocity", "body_force", "inlet_velocity", "equation", "kappa_sq", "dirichlet")
+    return {k: case[k] for k in keys if k in case}

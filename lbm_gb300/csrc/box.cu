@@ -36,51 +36,14 @@
 
 #include "box.h"
 #include "lattice.cuh"
+#include "step_common.cuh"
+#include "step_common.cuh"
 
 namespace lbm {
 namespace {
 
 constexpr uint8_t TYPE_MASK  = 0x07;
 constexpr uint8_t NEAR_SOLID = 0x08;  // set by the engine: a neighbour is solid
-constexpr float   DEV_SCALE  = 4096.0f;
-
-// ---- storage conversions ---------------------------------------------------
-template <int ST>
-struct Store;
-template <>
-struct Store<LBM_STORE_F64> {
-  using T = double;
-  using C = double;
-  static constexpr bool DEV = false;
-  static __device__ __forceinline__ C load(T v, C) { return v; }
-  static __device__ __forceinline__ T store(C f, C) { return f; }
-};
-template <>
-struct Store<LBM_STORE_F32> {
-  using T = float;
-  using C = float;
-  static constexpr bool DEV = true;  // holds f - w
-  static __device__ __forceinline__ C load(T v, C) { return v; }
-  static __device__ __forceinline__ T store(C d, C) { return d; }
-};
-template <>
-struct Store<LBM_STORE_F16_DEV> {
-  using T = __half;
-  using C = float;
-  static constexpr bool DEV = true;
-  // deviation d = w * h / 2^12
-  static __device__ __forceinline__ C load(T v, C w) { return __half2float(v) * (w * (1.0f / DEV_SCALE)); }
-  static __device__ __forceinline__ T store(C d, C w) { return __float2half_rn(d * (DEV_SCALE / w)); }
-};
-template <>
-struct Store<LBM_STORE_BF16_DEV> {
-  using T = __nv_bfloat16;
-  using C = float;
-  static constexpr bool DEV = true;
-  static __device__ __forceinline__ C load(T v, C w) { return __bfloat162float(v) * (w * (1.0f / DEV_SCALE)); }
-  static __device__ __forceinline__ T store(C d, C w) { return __float2bfloat16_rn(d * (DEV_SCALE / w)); }
-};
-
 // ---- link resolution ---------------------------------------------------------
 // mirror of direction q in the axes of `mask` (free-slip reflection)
 template <int LAT>
@@ -137,7 +100,8 @@ __device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z,
         double cu = 0;
 #pragma unroll
         for(int d = 0; d < L::D; ++d) cu += static_cast<double>(L::c(arrive, d)) * P.wall_u[face][d];
-        corr += 6.0 * L::w(arrive) * cu;  // 2 w (c.u_w) / c_s^2 with rho_w = 1
+        // 2 w (c.u_w) / c_s^2 with rho_w = 1, in state units S (delta f) / w
+        corr += 6.0 * STATE_SCALE * cu;
       }
     }
   }
@@ -170,143 +134,61 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
   return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
 }
 
-// ---- compile-time loops over the directions ------------------------------
-// Every per-direction statement of the step is instantiated with a constant q,
-// so lattice velocities, weights and plane offsets fold into immediates and
-// the populations stay in registers.
-template <class F, int... Is>
-__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {
-  (f(std::integral_constant<int, Is>{}), ...);
-}
-template <int N, class F>
-__device__ __forceinline__ void static_for(F&& f) {
-  static_for_impl(f, std::make_integer_sequence<int, N>{});
-}
-
-// ---- collision -------------------------------------------------------------
-// f (or its deviation from w for DEV storage) in, post-collision out
-template <int LAT, int EQ, class C, bool DEV>
-__device__ __forceinline__ void collide(const BoxParams& P, C* f, C* mom_out) {
-  using L         = Lattice<LAT>;
-  constexpr int Q = L::Q, D = L::D;
-  const C       omega = static_cast<C>(P.omega);
+template <int LAT, int EQ, class C>
+__device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
   if constexpr(EQ == LBM_NAVIER_STOKES) {
-    C rho0 = 0, j[3] = {0, 0, 0};
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      rho0 += f[q];
-      static_for<D>([&](auto dc) {
-        constexpr int d = decltype(dc)::value;
-        if constexpr(L::c(q, d) > 0) j[d] += f[q];
-        if constexpr(L::c(q, d) < 0) j[d] -= f[q];
-      });
-    });
-    // DEV: rho0 is rho - 1 (sum of deviations), j is exact since sum c w = 0
-    const C rho  = DEV ? C(1) + rho0 : rho0;
-    const C irho = C(1) / rho;
-    C       u[3] = {0, 0, 0};
-    C       F[3] = {0, 0, 0};
-    const bool force = P.has_force != 0;
-    if(force) {
-      static_for<D>([&](auto dc) { F[decltype(dc)::value] = static_cast<C>(P.force[decltype(dc)::value]); });
-    }
-    static_for<D>([&](auto dc) {
-      constexpr int d = decltype(dc)::value;
-      u[d]            = (j[d] + C(0.5) * F[d]) * irho;
-    });
-    C usq = 0;
-    static_for<D>([&](auto dc) { usq += u[decltype(dc)::value] * u[decltype(dc)::value]; });
-    if(mom_out) {
-      mom_out[0] = rho;
-      static_for<D>([&](auto dc) { mom_out[1 + decltype(dc)::value] = u[decltype(dc)::value]; });
-    }
-    const C guo = C(1) - C(0.5) * omega;
-    // feq - w = w (rho - 1 + rho (3 cu + 4.5 cu^2 - 1.5 u^2)) for DEV storage
-    const C k0 = DEV ? rho0 - rho * C(1.5) * usq : rho * (C(1) - C(1.5) * usq);
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      C             cu = 0;
-      static_for<D>([&](auto dc) {
-        constexpr int d = decltype(dc)::value;
-        if constexpr(L::c(q, d) > 0) cu += u[d];
-        if constexpr(L::c(q, d) < 0) cu -= u[d];
-      });
-      constexpr C w   = static_cast<C>(L::w(q));
-      const C     feq = w * (k0 + rho * cu * (C(3) + C(4.5) * cu));
-      C           out = f[q] + omega * (feq - f[q]);
-      if(force) {
-        C cf = 0, uf = 0;
-        static_for<D>([&](auto dc) {
-          constexpr int d = decltype(dc)::value;
-          cf += static_cast<C>(L::c(q, d)) * F[d];
-          uf += u[d] * F[d];
-        });
-        out += guo * w * (C(3) * (cf - uf) + C(9) * cu * cf);
-      }
-      f[q] = out;
-    });
+    C F[3];
+    F[0] = prm<C>(P.force[0], P.force_f[0]);
+    F[1] = prm<C>(P.force[1], P.force_f[1]);
+    F[2] = prm<C>(P.force[2], P.force_f[2]);
+    collide_ns<LAT, C>(prm<C>(P.omega, P.omega_f), P.has_force != 0, F, v, mom_out);
   } else {
-    // Poisson(-Boltzmann), Chai & Shi: phi from the moving populations
-    C acc = 0;
-    static_for<Q - 1>([&](auto qc) { acc += f[decltype(qc)::value]; });
-    const C phi = acc * static_cast<C>(1.0 / (1.0 - L::w(Q - 1)));
-    if(mom_out) mom_out[0] = phi;
-    const C g   = P.pb_nonlinear ? static_cast<C>(sinh(static_cast<double>(phi))) : phi;
-    const C src = static_cast<C>(P.pb_diffusivity * P.kappa_sq) * g;
-    static_for<Q>([&](auto qc) {
-      constexpr int q   = decltype(qc)::value;
-      const C       feq = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
-      C             out = f[q] + omega * (feq - f[q]);
-      if constexpr(q != Q - 1) out += static_cast<C>(L::pw(q)) * src;
-      f[q] = out;
-    });
+    collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
+                            mom_out);
   }
 }
 
-// equilibrium emitted by inlet / Dirichlet cells (deviation for DEV storage)
-template <int LAT, int EQ, class C, bool DEV>
-__device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* f, int64_t cell) {
+// state emitted by inlet / Dirichlet cells
+template <int LAT, int EQ, class C>
+__device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* v, int64_t cell) {
   using L         = Lattice<LAT>;
   constexpr int Q = L::Q, D = L::D;
   if constexpr(EQ == LBM_NAVIER_STOKES) {
-    const C rho = static_cast<C>(P.inlet_rho);
-    C       usq = 0;
-    static_for<D>([&](auto dc) { usq += static_cast<C>(P.inlet_u[decltype(dc)::value] * P.inlet_u[decltype(dc)::value]); });
+    const C rho = prm<C>(P.inlet_rho, P.inlet_rho_f);
+    C       ui[3];
+    static_for<D>([&](auto dc) { ui[decltype(dc)::value] = prm<C>(P.inlet_u[decltype(dc)::value], P.inlet_u_f[decltype(dc)::value]); });
+    C usq = 0;
+    static_for<D>([&](auto dc) { usq += ui[decltype(dc)::value] * ui[decltype(dc)::value]; });
     static_for<Q>([&](auto qc) {
       constexpr int q  = decltype(qc)::value;
       C             cu = 0;
       static_for<D>([&](auto dc) {
         constexpr int d = decltype(dc)::value;
-        cu += static_cast<C>(L::c(q, d)) * static_cast<C>(P.inlet_u[d]);
+        cu += static_cast<C>(L::c(q, d)) * ui[d];
       });
-      const C w    = static_cast<C>(L::w(q));
       const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
-      f[q]         = DEV ? w * ((rho - C(1)) + rho * poly) : w * rho * (C(1) + poly);
+      v[q]         = static_cast<C>(STATE_SCALE) * ((rho - C(1)) + rho * poly);
     });
   } else {
     const C phi = P.dirichlet ? static_cast<C>(P.dirichlet[cell]) : C(0);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      f[q]            = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+      v[q]            = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
     });
   }
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block sum of the per-thread residual contributions into partials[k*stride + slot]
-template <int NV>
-__device__ __forceinline__ void block_partials(const double* diff, double* partials, int64_t stride, int64_t slot) {
+// block sum of the per-thread residual contributions into partials[k*stride + slot].
+// The warp level runs in the arithmetic type C (FP32 storages keep it off the
+// narrow FP64 pipe); warp sums and everything after them are FP64.
+template <int NV, class C>
+__device__ __forceinline__ void block_partials(const C* diff, double* partials, int64_t stride, int64_t slot) {
   __shared__ double red[NV][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for(int k = 0; k < NV; ++k) {
-    const double s = warp_sum(diff[k]);
-    if(lane == 0) red[k][wid] = s;
+    const C s = warp_sum(diff[k]);
+    if(lane == 0) red[k][wid] = static_cast<double>(s);
   }
   __syncthreads();
   if(wid == 0) {
@@ -320,12 +202,12 @@ __device__ __forceinline__ void block_partials(const double* diff, double* parti
 }
 
 template <int LAT, int EQ, class C, int MOM, int NV>
-__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, double* diff) {
+__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, C* diff) {
   if constexpr(MOM != 0) {
     C* M = static_cast<C*>(P.mom);
 #pragma unroll
     for(int k = 0; k < NV; ++k) {
-      if constexpr(MOM == 2) diff[k] = fabs(static_cast<double>(mom[k]) - static_cast<double>(M[k * P.ncells + cell]));
+      if constexpr(MOM == 2) diff[k] = fabs(mom[k] - M[k * P.ncells + cell]);
       M[k * P.ncells + cell] = mom[k];
     }
   }
@@ -349,7 +231,6 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
   constexpr int NV   = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
 
   const int  x     = blockIdx.x * blockDim.x + threadIdx.x;
@@ -361,9 +242,9 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   const uint8_t type = flag & TYPE_MASK;
   T*            A    = static_cast<T*>(P.pop);
   const int     NA   = static_cast<int>(P.nalloc);
-  double        diff[NV];
+  C             diff[NV];
 #pragma unroll
-  for(int k = 0; k < NV; ++k) diff[k] = 0.0;
+  for(int k = 0; k < NV; ++k) diff[k] = C(0);
 
   bool work;
   if constexpr(ODD) work = type == LBM_CELL_FLUID && !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
@@ -376,18 +257,18 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
     for(int k = 0; k < NV; ++k) mom[k] = 0;
     const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     if(emit) {
-      emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+      emit_equilibrium<LAT, EQ, C>(P, f, cell);
     } else {
       if constexpr(!ODD) {
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          f[q]            = S::load(A[q * NA + cell], static_cast<C>(L::w(q)));
+          f[q]            = S::load(A[q * NA + cell]);
         });
         if(type == LBM_CELL_OUTLET) {
           // links from beyond +x: what the upstream cell received (ghost plane)
           static_for<Q>([&](auto qc) {
             constexpr int q = decltype(qc)::value;
-            if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], static_cast<C>(L::w(q)));
+            if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
           });
         }
       } else {
@@ -395,23 +276,23 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
         static_for<Q>([&](auto qc) {
           constexpr int q   = decltype(qc)::value;
           const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-          f[q]              = S::load(A[L::opp(q) * NA + cell - off], static_cast<C>(L::w(q)));
+          f[q]              = S::load(A[L::opp(q) * NA + cell - off]);
         });
       }
-      collide<LAT, EQ, C, DEV>(P, f, MOM ? mom : nullptr);
+      collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
     }
     moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
     if constexpr(!ODD) {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        A[L::opp(q) * NA + cell] = S::store(f[q], static_cast<C>(L::w(L::opp(q))));
+        A[L::opp(q) * NA + cell] = S::store(f[q]);
       });
     } else {
       const int sy = P.nx, sz = P.nx * P.ny;
       static_for<Q>([&](auto qc) {
         constexpr int q   = decltype(qc)::value;
         const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-        A[q * NA + cell + off] = S::store(f[q], static_cast<C>(L::w(q)));
+        A[q * NA + cell + off] = S::store(f[q]);
       });
     }
   }
@@ -421,56 +302,78 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   }
 }
 
+// Link tables of the boundary cells, built once: for list entry i and
+// direction q, src[q*n+i] is the population slot the odd step pulls into f_q
+// (a neighbour's slot, the cell's own slot for a bounce, or the outlet ghost)
+// and dst[q*n+i] the slot the post-collision f_q is pushed to (-1: it leaves
+// through an open face).  corr_* hold the moving-wall momentum in state units
+// (only allocated when a wall moves).
+template <int LAT>
+__global__ void k_box_build_links(BoxParams P, const int32_t* list, int n, int32_t* src, int32_t* dst, double* corr_src,
+                                  double* corr_dst) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q;
+  const int     i = blockIdx.x * blockDim.x + threadIdx.x;
+  if(i >= n) return;
+  const int     cell = list[i];
+  const int     x = cell % P.nx, y = (cell / P.nx) % P.ny, z = cell / (P.nx * P.ny);
+  const int64_t NA   = P.nalloc;
+  static_for<Q>([&](auto qc) {
+    constexpr int q  = decltype(qc)::value;
+    const Link    lp = resolve<LAT>(P, x, y, z, q, -1, q);
+    int64_t       s;
+    if(lp.kind == LINK_CELL) s = L::opp(lp.q) * NA + lp.cell;
+    else if(lp.kind == LINK_BOUNCE) s = q * NA + cell;
+    else s = Q * NA + ghost_index(P, q, y, z);
+    src[q * n + i] = static_cast<int32_t>(s);
+    const Link lq  = resolve<LAT>(P, x, y, z, q, +1, L::opp(q));
+    int64_t    d   = -1;
+    if(lq.kind == LINK_CELL) d = lq.q * NA + lq.cell;
+    else if(lq.kind == LINK_BOUNCE) d = L::opp(q) * NA + cell;
+    dst[q * n + i] = static_cast<int32_t>(d);
+    if(corr_src) {
+      corr_src[q * n + i] = lp.kind == LINK_BOUNCE ? lp.corr : 0.0;
+      corr_dst[q * n + i] = lq.kind == LINK_BOUNCE ? lq.corr : 0.0;
+    }
+  });
+}
+
 template <int LAT, int EQ, int ST, int MOM>
-__global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int n, int64_t slot0) {
+__global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int n, int64_t slot0, const int32_t* src,
+                                                 const int32_t* dst, const double* corr_src, const double* corr_dst) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
   constexpr int NV   = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
   const int     i    = blockIdx.x * blockDim.x + threadIdx.x;
-  double        diff[NV];
+  C             diff[NV];
 #pragma unroll
-  for(int k = 0; k < NV; ++k) diff[k] = 0.0;
+  for(int k = 0; k < NV; ++k) diff[k] = C(0);
   if(i < n) {
     const int     cell = list[i];
-    const int     x = cell % P.nx, y = (cell / P.nx) % P.ny, z = cell / (P.nx * P.ny);
     const uint8_t type = P.flags[cell] & TYPE_MASK;
     T*            A    = static_cast<T*>(P.pop);
-    const int64_t NA   = P.nalloc;
     C             f[Q];
     C             mom[NV];
 #pragma unroll
     for(int k = 0; k < NV; ++k) mom[k] = 0;
     if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
-      emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+      emit_equilibrium<LAT, EQ, C>(P, f, cell);
     } else {
       static_for<Q>([&](auto qc) {
-        constexpr int q  = decltype(qc)::value;
-        const Link    lk = resolve<LAT>(P, x, y, z, q, -1, q);
-        if(lk.kind == LINK_CELL) {
-          f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], static_cast<C>(L::w(q)));
-        } else if(lk.kind == LINK_BOUNCE) {
-          f[q] = S::load(A[q * NA + cell], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr);
-        } else {
-          f[q] = S::load(A[Q * NA + ghost_index(P, q, y, z)], static_cast<C>(L::w(q)));
-        }
+        constexpr int q = decltype(qc)::value;
+        f[q]            = S::load(A[src[q * n + i]]);
+        if(corr_src) f[q] += static_cast<C>(corr_src[q * n + i]);
       });
-      collide<LAT, EQ, C, DEV>(P, f, MOM ? mom : nullptr);
+      collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
     }
     moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
     static_for<Q>([&](auto qc) {
-      constexpr int q  = decltype(qc)::value;
-      const Link    lk = resolve<LAT>(P, x, y, z, q, +1, L::opp(q));
-      if(lk.kind == LINK_CELL) {
-        A[lk.q * NA + lk.cell] = S::store(f[q], static_cast<C>(L::w(lk.q)));
-      } else if(lk.kind == LINK_BOUNCE) {
-        constexpr int o   = L::opp(q);
-        A[o * NA + cell] = S::store(f[q] + static_cast<C>(lk.corr), static_cast<C>(L::w(o)));
-      }
-      // LINK_OPEN: the population leaves the box
+      constexpr int q = decltype(qc)::value;
+      const int32_t d = dst[q * n + i];
+      if(d >= 0) A[d] = S::store(corr_dst ? f[q] + static_cast<C>(corr_dst[q * n + i]) : f[q]);
     });
   }
   if constexpr(MOM == 2) block_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x);
@@ -506,7 +409,7 @@ __global__ void k_box_outlet(BoxParams P) {
       } else {
         // bounce-back at the upstream cell (a wall or solid beside it)
         using C = typename S::C;
-        v = S::store(S::load(A[q * NA + u], static_cast<C>(L::w(q))) + static_cast<C>(lk.corr), static_cast<C>(L::w(q)));
+        v = S::store(S::load(A[q * NA + u]) + static_cast<C>(lk.corr));
       }
     }
     A[Q * NA + ghost_index(P, q, y, z)] = v;
@@ -523,7 +426,6 @@ __global__ void k_box_readout(BoxParams P, bool odd, double* out) {
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
   if(x >= P.nx) return;
   const int64_t cell = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
@@ -537,14 +439,13 @@ __global__ void k_box_readout(BoxParams P, bool odd, double* out) {
     return;
   }
   if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
-    emit_equilibrium<LAT, EQ, C, DEV>(P, f, cell);
+    emit_equilibrium<LAT, EQ, C>(P, f, cell);
   } else {
 #pragma unroll
     for(int q = 0; q < Q; ++q) {
-      const C w = static_cast<C>(L::w(q));
       if(!odd) {
-        f[q] = S::load(A[q * NA + cell], w);
-        if(type == LBM_CELL_OUTLET && L::c(q, 0) < 0) f[q] = S::load(A[q * NA + cell - 1], w);
+        f[q] = S::load(A[q * NA + cell]);
+        if(type == LBM_CELL_OUTLET && L::c(q, 0) < 0) f[q] = S::load(A[q * NA + cell - 1]);
       } else {
         int  xs = x;
         Link lk = resolve<LAT>(P, x, y, z, q, -1, q);
@@ -553,13 +454,13 @@ __global__ void k_box_readout(BoxParams P, bool odd, double* out) {
           lk = resolve<LAT>(P, xs, y, z, q, -1, q);
         }
         const int64_t own = xs + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
-        if(lk.kind == LINK_CELL) f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], w);
-        else f[q] = S::load(A[q * NA + own], w) + static_cast<C>(lk.corr);
+        if(lk.kind == LINK_CELL) f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell]);
+        else f[q] = S::load(A[q * NA + own]) + static_cast<C>(lk.corr);
       }
     }
   }
 #pragma unroll
-  for(int q = 0; q < Q; ++q) out[q * N + cell] = static_cast<double>(f[q]) + (DEV ? L::w(q) : 0.0);
+  for(int q = 0; q < Q; ++q) out[q * N + cell] = state_to_f<LAT, EQ>(static_cast<double>(f[q]), q);
 }
 
 // store FP64 post-stream populations into the standard (even-parity) layout
@@ -570,14 +471,12 @@ __global__ void k_box_load(BoxParams P, const double* in) {
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
   const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if(cell >= P.ncells) return;
   T* A = static_cast<T*>(P.pop);
 #pragma unroll
   for(int q = 0; q < Q; ++q) {
-    const double v = in[q * P.ncells + cell] - (DEV ? L::w(q) : 0.0);
-    A[q * P.nalloc + cell] = S::store(static_cast<C>(v), static_cast<C>(L::w(q)));
+    A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(in[q * P.ncells + cell], q)));
   }
 }
 
@@ -592,12 +491,11 @@ __global__ void k_box_init(BoxParams P, InitVec v) {
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr bool DEV = S::DEV && EQ == LBM_NAVIER_STOKES;
   const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if(cell >= P.ncells) return;
   T* A = static_cast<T*>(P.pop);
 #pragma unroll
-  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(v.f[q] - (DEV ? L::w(q) : 0.0)), static_cast<C>(L::w(q)));
+  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(v.f[q], q)));
 }
 
 // moments (rho or phi, u) of FP64 populations
@@ -666,6 +564,27 @@ __global__ void k_box_sum(const double* f, int64_t n, double* partials) {
   }
 }
 
+// first level of the residual reduction: block c sums the contiguous chunk
+// [c*chunk, (c+1)*chunk) of every vector into mid[v*gridDim.x + c]
+__global__ void k_chunk_sum(const double* partials, int64_t nb, int64_t stride, int nvec, int64_t chunk, double* mid) {
+  __shared__ double sh[32];
+  const int64_t lo = blockIdx.x * chunk, hi = lo + chunk < nb ? lo + chunk : nb;
+  for(int v = 0; v < nvec; ++v) {
+    double acc = 0;
+    for(int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) acc += partials[v * stride + i];
+    acc = warp_sum(acc);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if(lane == 0) sh[wid] = acc;
+    __syncthreads();
+    if(wid == 0) {
+      double t = lane < static_cast<int>(blockDim.x >> 5) ? sh[lane] : 0.0;
+      t        = warp_sum(t);
+      if(lane == 0) mid[v * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_final_sum(const double* partials, int64_t nb, int64_t stride, int nvec, double* out) {
   __shared__ double sh[32];
   for(int v = 0; v < nvec; ++v) {
@@ -706,9 +625,9 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
     if(nbb) {
-      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
-      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
-      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk);
+      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
     }
     if(mom == 2) b->res_slots = nbulk + nbb;
   } else {
@@ -865,7 +784,10 @@ int box_residual(BoxState* b, double* r, cudaStream_t s, std::string& err) {
     err = "residual needs a step call of at least two steps";
     return LBM_ERR_INVALID;
   }
-  k_final_sum<<<1, 256, 0, s>>>(b->partials, b->res_slots, b->p.partial_stride, b->nvar, b->out);
+  // two levels, fixed shapes: deterministic bits for a given box and tuning
+  const int64_t chunk = (b->res_slots + kMidBlocks - 1) / kMidBlocks;
+  k_chunk_sum<<<kMidBlocks, 256, 0, s>>>(b->partials, b->res_slots, b->p.partial_stride, b->nvar, chunk, b->partials_mid);
+  k_final_sum<<<1, 256, 0, s>>>(b->partials_mid, kMidBlocks, kMidBlocks, b->nvar, b->out);
   cudaError_t e = cudaMemcpyAsync(r, b->out, sizeof(double) * b->nvar, cudaMemcpyDeviceToHost, s);
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return cerr(err, e, "residual");
@@ -940,6 +862,10 @@ void box_destroy(BoxState* b) {
   cudaFree(b->out);
   cudaFree(b->f64);
   cudaFree(b->bnd_list);
+  cudaFree(b->link_src);
+  cudaFree(b->link_dst);
+  cudaFree(b->corr_src);
+  cudaFree(b->corr_dst);
   delete b;
 }
 
@@ -1063,6 +989,13 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   p.pb_diffusivity = Lattice<LBM_D3Q7>::poisson_alpha * (0.5 - 1.0 / desc->omega);
   p.has_outlet = has_outlet ? 1 : 0;
   p.mom_mode   = 0;
+  p.omega_f     = static_cast<float>(p.omega);
+  p.inlet_rho_f = static_cast<float>(p.inlet_rho);
+  p.pb_src_f    = static_cast<float>(p.pb_diffusivity * p.kappa_sq);
+  for(int d = 0; d < 3; ++d) {
+    p.force_f[d]   = static_cast<float>(p.force[d]);
+    p.inlet_u_f[d] = static_cast<float>(p.inlet_u[d]);
+  }
 
   cudaError_t e = cudaMalloc(&b->pop, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
   if(e == cudaSuccess) e = cudaMemset(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
@@ -1103,8 +1036,9 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   if(e == cudaSuccess) e = cudaMemset(b->mom, 0, csize * b->nvar * ncells);
   // partials for the largest launch (smallest block size considered by the tuner)
   const int64_t maxblocks = static_cast<int64_t>((desc->nx + 63) / 64) * desc->ny * desc->nz + (b->n_bnd + 127) / 128;
-  if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4));
+  if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4 + kMidBlocks * 4));
   b->partials_mm      = b->partials + maxblocks * 4;
+  b->partials_mid     = b->partials_mm + 304 * 4;
   p.partial_stride    = maxblocks;
   if(e == cudaSuccess) e = cudaMalloc(&b->out, sizeof(double) * 8);
   p.flags     = b->flags;
@@ -1112,6 +1046,27 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   p.pop       = b->pop;
   p.mom       = b->mom;
   p.partials  = b->partials;
+  bool moving = false;
+  for(int i = 0; i < 6; ++i)
+    for(int d = 0; d < 3; ++d)
+      if(desc->wall_velocity[i][d] != 0.0 && desc->face[i] == LBM_FACE_WALL) moving = true;
+  if(e == cudaSuccess && b->n_bnd > 0) {
+    const size_t nl = static_cast<size_t>(b->n_bnd) * b->Q;
+    e = cudaMalloc(&b->link_src, sizeof(int32_t) * nl);
+    if(e == cudaSuccess) e = cudaMalloc(&b->link_dst, sizeof(int32_t) * nl);
+    if(e == cudaSuccess && moving) e = cudaMalloc(&b->corr_src, sizeof(double) * nl);
+    if(e == cudaSuccess && moving) e = cudaMalloc(&b->corr_dst, sizeof(double) * nl);
+    if(e == cudaSuccess) {
+      const unsigned g = static_cast<unsigned>((b->n_bnd + 127) / 128);
+      const int      n = static_cast<int>(b->n_bnd);
+      switch(lat) {
+        case LBM_D2Q9: k_box_build_links<LBM_D2Q9><<<g, 128>>>(p, b->bnd_list, n, b->link_src, b->link_dst, b->corr_src, b->corr_dst); break;
+        case LBM_D3Q19: k_box_build_links<LBM_D3Q19><<<g, 128>>>(p, b->bnd_list, n, b->link_src, b->link_dst, b->corr_src, b->corr_dst); break;
+        default: k_box_build_links<LBM_D3Q7><<<g, 128>>>(p, b->bnd_list, n, b->link_src, b->link_dst, b->corr_src, b->corr_dst); break;
+      }
+      e = cudaDeviceSynchronize();
+    }
+  }
   cudaStream_t stream = nullptr;
   if(e == cudaSuccess) e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
   if(e != cudaSuccess) {

@@ -14,6 +14,9 @@ struct lbm_gpu_ctx;
 
 namespace lbm {
 
+// blocks of the first level of the residual reduction (two per SM on 152 SMs)
+constexpr int kMidBlocks = 304;
+
 // Everything a box kernel needs, passed by value (kernel parameter space).
 struct BoxParams {
   int     nx, ny, nz;       // fluid box
@@ -28,6 +31,9 @@ struct BoxParams {
   double  pb_diffusivity;   // alpha (1/2 - tau) in lattice units
   int     pb_nonlinear;
   int     has_force;
+  // single-precision copies for the FP32-arithmetic kernels (GB300's FP64
+  // pipe is narrow: converting a double parameter per cell is measurable)
+  float   omega_f, force_f[3], inlet_rho_f, inlet_u_f[3], pb_src_f;
   int     has_outlet;
   const uint8_t* flags;     // ncells
   const double*  dirichlet; // ncells Poisson Dirichlet values or nullptr
@@ -51,6 +57,7 @@ struct BoxState {
   void*        mom   = nullptr;
   double*      partials = nullptr;     // residual partials (one per step block and variable)
   double*      partials_mm = nullptr;  // mass / momentum partials
+  double*      partials_mid = nullptr; // first-level residual sums (kMidBlocks per variable)
   double*      out   = nullptr;
   double*      f64   = nullptr;  // FP64 staging for transfers (Q x ncells)
   int          res_ready = 0;  // partials hold the residual of the last step
@@ -58,6 +65,10 @@ struct BoxState {
   int          tuned_tpb = 128;
   int32_t*     bnd_list  = nullptr;  // cells the odd step resolves link by link
   int64_t      n_bnd     = 0;
+  int32_t*     link_src  = nullptr;  // n_bnd x Q pull slots of the boundary cells
+  int32_t*     link_dst  = nullptr;  // n_bnd x Q push slots (-1: leaves the box)
+  double*      corr_src  = nullptr;  // moving-wall terms (allocated only when a wall moves)
+  double*      corr_dst  = nullptr;
   int64_t      res_slots = 0;        // partial slots written by the last residual step
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
 };

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "box.h"
 #include "engine.h"
 #include "lattice.cuh"
@@ -37,7 +38,7 @@ struct HostBnd {
 };
 
 struct lbm_gpu_ctx {
-  int                    mode   = 0;  // 0 reference tables, 1 dense box
+  int                    mode   = 0;  // 0 reference tables, 1 dense box, 2 batched cavities
   int                    device = 0;
   cudaStream_t           stream = nullptr;
   std::string            err;
@@ -56,6 +57,7 @@ struct lbm_gpu_ctx {
   cudaGraphExec_t        graph      = nullptr;
   int                    graph_steps = 0;
   BoxState*              box        = nullptr;
+  BatchState*            batch      = nullptr;
 };
 
 namespace {
@@ -604,6 +606,7 @@ int lbm_gpu_set_forcing(lbm_gpu_ctx* ctx, double dp, int64_t nin, const int64_t*
 int lbm_gpu_initial_condition(lbm_gpu_ctx* ctx) {
   if(!ctx) return LBM_ERR_INVALID;
   if(ctx->mode == 1) return box_initial_condition(ctx->box, ctx->stream) == cudaSuccess ? LBM_OK : fail(ctx, LBM_ERR_CUDA, "box init");
+  if(ctx->mode == 2) return batch_initial_condition(ctx->batch, ctx->stream) == cudaSuccess ? LBM_OK : fail(ctx, LBM_ERR_CUDA, "batch init");
   CK(cudaSetDevice(ctx->device));
   TableState&         t = ctx->t;
   const int64_t       n = t.n;
@@ -636,10 +639,8 @@ int lbm_gpu_step(lbm_gpu_ctx* ctx, int64_t nsteps) {
   if(!ctx || nsteps < 0) return LBM_ERR_INVALID;
   CK(cudaSetDevice(ctx->device));
   if(nsteps == 0) return LBM_OK;
-  if(ctx->mode == 1) {
-    const int rc = box_step(ctx->box, nsteps, ctx->stream, ctx->err);
-    return rc;
-  }
+  if(ctx->mode == 1) return box_step(ctx->box, nsteps, ctx->stream, ctx->err);
+  if(ctx->mode == 2) return batch_step(ctx->batch, nsteps, ctx->stream, ctx->err);
   // the step's kernel sequence is captured once as a graph of G steps
   const int G = 8;
   if(!ctx->graph) {
@@ -669,6 +670,7 @@ int lbm_gpu_residual(lbm_gpu_ctx* ctx, double* r) {
   if(!ctx || !r) return LBM_ERR_INVALID;
   CK(cudaSetDevice(ctx->device));
   if(ctx->mode == 1) return box_residual(ctx->box, r, ctx->stream, ctx->err);
+  if(ctx->mode == 2) return fail(ctx, LBM_ERR_INVALID, "batched contexts report residuals per cavity (lbm_gpu_batch_residuals)");
   TableState& t = ctx->t;
   CK(reduce_abs_diff(t.vars, t.varsold, t.n, t.nvar, ctx->d_partials, ctx->nblocks, ctx->d_out, ctx->stream));
   CK(cudaMemcpyAsync(r, ctx->d_out, sizeof(double) * t.nvar, cudaMemcpyDeviceToHost, ctx->stream));
@@ -724,12 +726,14 @@ int lbm_gpu_get_populations(lbm_gpu_ctx* ctx, double* fold) {
   if(!ctx || !fold) return LBM_ERR_INVALID;
   CK(cudaSetDevice(ctx->device));
   if(ctx->mode == 1) return box_get_populations(ctx->box, fold, ctx->stream, ctx->err);
+  if(ctx->mode == 2) return fail(ctx, LBM_ERR_INVALID, "batched contexts: lbm_gpu_batch_get_domain");
   return soa_io(ctx, ctx->t.fold, ctx->t.Q, fold, nullptr);
 }
 int lbm_gpu_set_populations(lbm_gpu_ctx* ctx, const double* fold) {
   if(!ctx || !fold) return LBM_ERR_INVALID;
   CK(cudaSetDevice(ctx->device));
   if(ctx->mode == 1) return box_set_populations(ctx->box, fold, ctx->stream, ctx->err);
+  if(ctx->mode == 2) return fail(ctx, LBM_ERR_INVALID, "batched contexts cannot take a whole-state upload");
   return soa_io(ctx, ctx->t.fold, ctx->t.Q, nullptr, fold);
 }
 
@@ -737,6 +741,7 @@ int lbm_gpu_reduce_mass_momentum(lbm_gpu_ctx* ctx, double* out) {
   if(!ctx || !out) return LBM_ERR_INVALID;
   CK(cudaSetDevice(ctx->device));
   if(ctx->mode == 1) return box_mass_momentum(ctx->box, out, ctx->stream, ctx->err);
+  if(ctx->mode == 2) return fail(ctx, LBM_ERR_INVALID, "batched contexts: not available");
   TableState& t = ctx->t;
   CK(reduce_moments(t.fold, t.n, t.Q, t.lattice, ctx->d_partials, ctx->nblocks, ctx->d_out, ctx->stream));
   CK(cudaMemcpyAsync(out, ctx->d_out, sizeof(double) * (t.D + 1), cudaMemcpyDeviceToHost, ctx->stream));
@@ -754,6 +759,7 @@ int lbm_gpu_synchronize(lbm_gpu_ctx* ctx) {
 int lbm_gpu_info(const lbm_gpu_ctx* ctx, int64_t* ncells, int32_t* q, int32_t* nvar) {
   if(!ctx) return LBM_ERR_INVALID;
   if(ctx->mode == 1) return box_info(ctx->box, ncells, q, nvar);
+  if(ctx->mode == 2) return batch_info(ctx->batch, ncells, q, nvar);
   if(ncells) *ncells = ctx->t.n;
   if(q) *q = ctx->t.Q;
   if(nvar) *nvar = ctx->t.nvar;
@@ -766,6 +772,7 @@ void lbm_gpu_destroy(lbm_gpu_ctx* ctx) {
   if(ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_graph(ctx);
   if(ctx->box) box_destroy(ctx->box);
+  if(ctx->batch) batch_destroy(ctx->batch);
   for(void* p : ctx->allocs) cudaFree(p);
   if(ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -784,6 +791,16 @@ lbm_gpu_ctx* lbm_internal_new_box_ctx(int device, BoxState* box, cudaStream_t st
   return ctx;
 }
 BoxState* lbm_internal_box(lbm_gpu_ctx* ctx) { return ctx && ctx->mode == 1 ? ctx->box : nullptr; }
+lbm_gpu_ctx* lbm_internal_new_batch_ctx(int device, BatchState* batch, cudaStream_t stream) {
+  lbm_gpu_ctx* ctx = new(std::nothrow) lbm_gpu_ctx();
+  if(!ctx) return nullptr;
+  ctx->mode   = 2;
+  ctx->device = device;
+  ctx->batch  = batch;
+  ctx->stream = stream;
+  return ctx;
+}
+BatchState* lbm_internal_batch(lbm_gpu_ctx* ctx) { return ctx && ctx->mode == 2 ? ctx->batch : nullptr; }
 cudaStream_t lbm_internal_stream(lbm_gpu_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
 void lbm_internal_set_error(lbm_gpu_ctx* ctx, const std::string& msg) {
   if(ctx) ctx->err = msg;

@@ -17,7 +17,7 @@ from typing import Dict, List, Optional
 import numpy as np
 
 from . import refconfig as rc
-from ._lib import BndDesc, BoxDesc, TableDesc, check, load
+from ._lib import BatchDesc, BndDesc, BoxDesc, TableDesc, check, load
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -358,3 +358,77 @@ class LBMSolver:
         passed = not (bounds["errorMax"] < max_err or bounds["errorL2"] < l2 or math.isnan(l2) or bounds["errorGRE"] < gre
                       or math.isnan(gre))
         return {"max": max_err, "l2": l2, "gre": gre, "bounds": bounds, "passed": passed}
+
+
+class BatchSolver:
+    """Many D2Q9 lid-driven cavities of different sizes, one launch per step."""
+
+    def __init__(self, sides, omegas, lid_velocity: float = 0.1, storage: str = "f32", device: int = 0):
+        lib = load()
+        self._lib = lib
+        self.ctx = None
+        self.sides = np.ascontiguousarray(sides, dtype=np.int32)
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        d = BatchDesc()
+        d.lattice, d.storage, d.device, d.ndomains, d.lid_velocity = rc.LATTICES["D2Q9"], STORAGE[storage], device, self.sides.size, lid_velocity
+        h = C.c_void_p()
+        check(lib.lbm_gpu_create_batch(C.byref(d), _ptr(self.sides), _ptr(om), C.byref(h)), None, "lbm_gpu_create_batch")
+        self.ctx = h
+        self.ndomains = self.sides.size
+        self.ncells = int(np.sum(self.sides.astype(np.int64) ** 2))
+
+    def close(self):
+        if self.ctx:
+            self._lib.lbm_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initial_condition(self):
+        check(self._lib.lbm_gpu_initial_condition(self.ctx), self.ctx, "initial_condition")
+
+    def step(self, n: int = 1):
+        check(self._lib.lbm_gpu_step(self.ctx, int(n)), self.ctx, "step")
+
+    def residuals(self) -> np.ndarray:
+        r = np.zeros(self.ndomains * 3)
+        check(self._lib.lbm_gpu_batch_residuals(self.ctx, _ptr(r)), self.ctx, "batch_residuals")
+        return r.reshape(self.ndomains, 3)
+
+    ACTIVE, CONVERGED, DIVERGED = 0, 1, 2
+
+    def run(self, max_steps: int, check_interval: int, tol: float, raise_on_divergence: bool = True) -> np.ndarray:
+        """Steps taken per cavity.  A cavity whose residual turns NaN/Inf
+        stops; the others go on, and the call raises LBM_ERR_DIVERGED at the
+        end unless raise_on_divergence is False (then see status())."""
+        steps = np.zeros(self.ndomains, dtype=np.int64)
+        rc_ = self._lib.lbm_gpu_batch_run(self.ctx, int(max_steps), int(check_interval), float(tol), _ptr(steps))
+        if rc_ != 0 and not (rc_ == -5 and not raise_on_divergence):
+            check(rc_, self.ctx, "batch_run")
+        return steps
+
+    def status(self) -> np.ndarray:
+        st = np.zeros(self.ndomains, dtype=np.int32)
+        check(self._lib.lbm_gpu_batch_status(self.ctx, _ptr(st)), self.ctx, "batch_status")
+        return st
+
+    def domain_populations(self, d: int) -> np.ndarray:
+        n = int(self.sides[d])
+        f = np.zeros(9 * n * n)
+        check(self._lib.lbm_gpu_batch_get_domain(self.ctx, int(d), _ptr(f)), self.ctx, "batch_get_domain")
+        return f.reshape(9, n * n)
+
+    def profile_steps(self, n: int):
+        tot, ker, cnt = C.c_double(), C.c_double(), C.c_int64()
+        check(self._lib.lbm_gpu_batch_profile_steps(self.ctx, int(n), C.byref(tot), C.byref(ker), C.byref(cnt)), self.ctx,
+              "batch_profile_steps")
+        return tot.value, ker.value, cnt.value
+
+    def tuning(self):
+        g, t = C.c_int32(), C.c_int32()
+        check(self._lib.lbm_gpu_batch_tuning(self.ctx, C.byref(g), C.byref(t)), self.ctx, "batch_tuning")
+        return g.value, t.value

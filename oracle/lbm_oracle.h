@@ -98,6 +98,8 @@ void ora_box_destroy(ora_box* b);
  * kappa^2 and the sinh nonlinearity switch. */
 int ora_box_set_poisson(ora_box* b, double kappa_sq, int nonlinear, const double* phi_dirichlet);
 void ora_box_init_equilibrium(ora_box* b, double rho, const double* u);
+/* hold Navier-Stokes populations as deviations f - w (call before init) */
+int ora_box_set_deviation(ora_box* b, int on);
 void ora_box_step(ora_box* b, int64_t nsteps, int nthreads);
 /* post-stream populations (SoA, q-major: f[q*ncells+cell]) and moments */
 void ora_box_get(const ora_box* b, double* f_soa, double* rho, double* u);

@@ -77,6 +77,7 @@ struct ora_box {
   double   kappa_sq;
   int      nonlinear;
   double*  dirichlet;
+  int      dev;  /* Navier-Stokes state held as deviations f - w (see ora_box_set_deviation) */
   double*  f;    /* post-stream, q-major */
   double*  fs;   /* post-collision scratch */
 };
@@ -138,6 +139,18 @@ int ora_box_set_poisson(ora_box* b, double kappa_sq, int nonlinear, const double
   return 0;
 }
 
+/* Deviation form: the same BGK update with every population held as f - w_q,
+ * rho - 1 = sum (f - w) and j = sum c (f - w) (since sum c w = 0), and
+ * feq - w = w (rho - 1 + rho (3 c.u + 4.5 (c.u)^2 - 1.5 u^2)).  Algebraically
+ * identical to the plain form; its rounding errors are relative to the
+ * deviations instead of to f = O(w), which matters over tens of thousands
+ * of steps. */
+int ora_box_set_deviation(ora_box* b, int on) {
+  if(b->eq != ORA_NAVIER_STOKES) return -1;
+  b->dev = on ? 1 : 0;
+  return 0;
+}
+
 static void equilibrium(const ora_box* b, double rho, const double* u, double* feq) {
   const blat_t* L   = &b->L;
   double        usq = 0;
@@ -149,9 +162,21 @@ static void equilibrium(const ora_box* b, double rho, const double* u, double* f
   }
 }
 
+static void equilibrium_dev(const ora_box* b, double rho, const double* u, double* deq) {
+  const blat_t* L   = &b->L;
+  double        usq = 0;
+  for(int d = 0; d < L->D; ++d) usq += u[d] * u[d];
+  for(int q = 0; q < L->Q; ++q) {
+    double cu = 0;
+    for(int d = 0; d < L->D; ++d) cu += L->c[q][d] * u[d];
+    deq[q] = L->w[q] * ((rho - 1.0) + rho * (3.0 * cu + 4.5 * cu * cu - 1.5 * usq));
+  }
+}
+
 void ora_box_init_equilibrium(ora_box* b, double rho, const double* u) {
   double feq[19];
-  if(b->eq == ORA_NAVIER_STOKES) equilibrium(b, rho, u, feq);
+  if(b->eq == ORA_NAVIER_STOKES && b->dev) equilibrium_dev(b, rho, u, feq);
+  else if(b->eq == ORA_NAVIER_STOKES) equilibrium(b, rho, u, feq);
   else
     for(int q = 0; q < b->L.Q; ++q) feq[q] = 0.0;
   for(int q = 0; q < b->L.Q; ++q)
@@ -161,7 +186,8 @@ void ora_box_init_equilibrium(ora_box* b, double rho, const double* u) {
 static void emit(const ora_box* b, int64_t cell, double* out) {
   const blat_t* L = &b->L;
   if(b->eq == ORA_NAVIER_STOKES) {
-    equilibrium(b, b->inlet_rho, b->inlet_u, out);
+    if(b->dev) equilibrium_dev(b, b->inlet_rho, b->inlet_u, out);
+    else equilibrium(b, b->inlet_rho, b->inlet_u, out);
   } else {
     const double phi = b->dirichlet ? b->dirichlet[cell] : 0.0;
     for(int q = 0; q < L->Q; ++q) out[q] = q == L->Q - 1 ? (L->w[q] - 1.0) * phi : L->w[q] * phi;
@@ -178,10 +204,12 @@ static void collide_cell(const ora_box* b, const double* f, double* out) {
       rho += f[q];
       for(int d = 0; d < D; ++d) j[d] += L->c[q][d] * f[q];
     }
+    if(b->dev) rho += 1.0; /* f holds deviations: sum = rho - 1 */
     double u[3] = {0, 0, 0};
     for(int d = 0; d < D; ++d) u[d] = (j[d] + 0.5 * b->force[d]) / rho;
     double feq[19];
-    equilibrium(b, rho, u, feq);
+    if(b->dev) equilibrium_dev(b, rho, u, feq);
+    else equilibrium(b, rho, u, feq);
     for(int q = 0; q < Q; ++q) {
       double o = f[q] + om * (feq[q] - f[q]);
       if(b->has_force) {
@@ -299,11 +327,17 @@ void ora_box_step(ora_box* b, int64_t nsteps, int nthreads) {
 void ora_box_get(const ora_box* b, double* f_soa, double* rho, double* u) {
   const blat_t* L = &b->L;
   const int64_t N = b->ncells;
-  if(f_soa) memcpy(f_soa, b->f, sizeof(double) * L->Q * N);
+  if(f_soa) {
+    memcpy(f_soa, b->f, sizeof(double) * L->Q * N);
+    if(b->dev)
+      for(int q = 0; q < L->Q; ++q)
+        for(int64_t i = 0; i < N; ++i)
+          if(b->flags[i] != ORA_CELL_SOLID) f_soa[q * N + i] += L->w[q];
+  }
   for(int64_t cell = 0; cell < N; ++cell) {
     double r = 0, j[3] = {0, 0, 0}, acc = 0;
     for(int q = 0; q < L->Q; ++q) {
-      const double v = b->f[q * N + cell];
+      const double v = b->f[q * N + cell] + (b->dev && b->flags[cell] != ORA_CELL_SOLID ? L->w[q] : 0.0);
       r += v;
       if(q < L->Q - 1) acc += v;
       for(int d = 0; d < L->D; ++d) j[d] += L->c[q][d] * v;
@@ -318,4 +352,10 @@ void ora_box_get(const ora_box* b, double* f_soa, double* rho, double* u) {
   }
 }
 
-void ora_box_set(ora_box* b, const double* f_soa) { memcpy(b->f, f_soa, sizeof(double) * b->L.Q * b->ncells); }
+void ora_box_set(ora_box* b, const double* f_soa) {
+  memcpy(b->f, f_soa, sizeof(double) * b->L.Q * b->ncells);
+  if(b->dev)
+    for(int q = 0; q < b->L.Q; ++q)
+      for(int64_t i = 0; i < b->ncells; ++i)
+        if(b->flags[i] != ORA_CELL_SOLID) b->f[q * b->ncells + i] -= b->L.w[q];
+}

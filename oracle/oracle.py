@@ -67,6 +67,8 @@ def lib():
         L.ora_box_step.argtypes = [vp, i64, i32]
         L.ora_box_get.argtypes = [vp, vp, vp, vp]
         L.ora_box_set.argtypes = [vp, vp]
+        L.ora_box_set_deviation.argtypes = [vp, i32]
+        L.ora_box_set_deviation.restype = i32
         _lib = L
     return _lib
 
@@ -143,7 +145,8 @@ class BoxOracle:
     FACE = {"wall": 0, "periodic": 1, "freeslip": 2, "open": 3}
 
     def __init__(self, lattice, shape, omega, faces=("wall",) * 6, flags=None, wall_velocity=None, body_force=(0, 0, 0),
-                 inlet_velocity=(0, 0, 0), inlet_density=1.0, equation=0, kappa_sq=0.0, pb_nonlinear=True, dirichlet=None):
+                 inlet_velocity=(0, 0, 0), inlet_density=1.0, equation=0, kappa_sq=0.0, pb_nonlinear=True, dirichlet=None,
+                 deviation=False):
         L = lib()
         nx, ny, nz = (tuple(shape) + (1, 1))[:3]
         self.shape = (nx, ny, nz)
@@ -162,6 +165,8 @@ class BoxOracle:
                                   inlet_density)
         if not self.h:
             raise ValueError("oracle: unsupported box")
+        if deviation:
+            L.ora_box_set_deviation(self.h, 1)
         if equation == 1:
             di = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.float64).reshape(-1)
             self._keep.append(di)

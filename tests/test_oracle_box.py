@@ -1,0 +1,60 @@
+"""The oracle's box engine (CPU) against the reference's own fixtures.
+
+The box restatement covers features the reference lacks (D3Q19, D3Q7, Guo
+forcing, inlet/outlet, free slip); its 2D bounce-back limit is tied to the
+reference here, on the Couette fixtures, in both of its arithmetic forms:
+
+* plain form (populations f): relative L2 <= 1e-12 against the reference's
+  populations, and
+* deviation form (f - w_q, the form the GPU engine stores): the same bound,
+  and within 1e-13 of the plain form.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import box_index, load_case, rel_l2
+from lbm_gb300 import cases
+from lbm_gb300 import refconfig as rc
+
+
+def couette_oracle(name, deviation):
+    meta, solver, grid, out, consts, bnds, forcing = load_case(name)
+    ij, (nx, ny) = box_index(grid)
+    tv = [b for b in bnds if b.kind == rc.BND_WALL_BB_TANGENTIAL][0].scalar
+    wv = np.zeros((6, 3))
+    wv[3, 0] = tv
+    o = oracle.BoxOracle(rc.LATTICES["D2Q9"], (nx, ny, 1), consts.omega, faces=("periodic", "periodic", "wall", "wall", "wall", "wall"),
+                         wall_velocity=wv, deviation=deviation)
+    o.init_equilibrium()
+    o.step(meta["steps"])
+    idx = ij[:, 0] + nx * ij[:, 1]
+    return o.populations()[:, idx].T, out["fold"].reshape(grid.ncells, 9)
+
+
+@pytest.mark.parametrize("name", ["couette_1", "couette_50"])
+@pytest.mark.parametrize("deviation", [False, True])
+def test_box_oracle_matches_reference_couette(name, deviation):
+    f, ref = couette_oracle(name, deviation)
+    assert rel_l2(f, ref) <= 1e-12
+
+
+def test_deviation_form_tracks_plain_form():
+    plain, _ = couette_oracle("couette_50", False)
+    dev, _ = couette_oracle("couette_50", True)
+    assert rel_l2(dev, plain) <= 1e-13
+
+
+def test_deviation_form_on_a_forced_channel():
+    c = cases.poiseuille_guo(nx=32, ny=16)
+    kw = cases.box_kwargs(c)
+    a = oracle.BoxOracle(c["lattice"], c["shape"], c["omega"], **kw)
+    b = oracle.BoxOracle(c["lattice"], c["shape"], c["omega"], deviation=True, **kw)
+    a.init_equilibrium()
+    b.init_equilibrium()
+    a.step(500)
+    b.step(500)
+    assert rel_l2(b.populations(), a.populations()) <= 1e-13
+    ra, ua = a.moments()
+    rb, ub = b.moments()
+    assert np.abs(ra - rb).max() <= 1e-13
