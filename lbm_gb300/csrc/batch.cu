@@ -32,7 +32,8 @@ namespace {
 using L9 = Lattice<LBM_D2Q9>;
 constexpr int Q9 = 9, NV9 = 3;
 
-__device__ __forceinline__ double wsum(double v) {
+template <class V>
+__device__ __forceinline__ V wsum(V v) {
 #pragma unroll
   for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -70,12 +71,18 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
     const int         y = static_cast<int>(r / D.tiles_per_row);
     const int         x = static_cast<int>(r % D.tiles_per_row) * 32 + lane;
     const int         n = D.n;
-    double            diff[NV9] = {0.0, 0.0, 0.0};
+    C                 diff[NV9] = {C(0), C(0), C(0)};  // summed in the arithmetic type, stored as FP64
     if(x < n) {
       T*            Ad   = A + D.pop_off;
       const int64_t pl   = D.plane;
       const int     cell = x + n * y;
       C             v[Q9];
+      C             prev[NV9];  // previous moments, read with the populations
+      if constexpr(MOM == 2) {
+        const C* M = static_cast<const C*>(P.mom) + D.mom_off;
+#pragma unroll
+        for(int k = 0; k < NV9; ++k) prev[k] = M[k * pl + cell];
+      }
       const bool    fast = x > 0 && x < n - 1 && y > 0 && y < n - 1;
       if constexpr(!ODD) {
         static_for<Q9>([&](auto qc) { v[decltype(qc)::value] = S::load(Ad[decltype(qc)::value * pl + cell]); });
@@ -104,7 +111,7 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
         C* M = static_cast<C*>(P.mom) + D.mom_off;
 #pragma unroll
         for(int k = 0; k < NV9; ++k) {
-          if(MOM == 2) diff[k] = fabs(static_cast<double>(mom[k]) - static_cast<double>(M[k * pl + cell]));
+          if constexpr(MOM == 2) diff[k] = fabs(mom[k] - prev[k]);
           M[k * pl + cell] = mom[k];
         }
       }
@@ -136,8 +143,8 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
     if constexpr(MOM == 2) {
 #pragma unroll
       for(int k = 0; k < NV9; ++k) {
-        const double s = wsum(diff[k]);
-        if(lane == 0) P.partials[k * P.partial_stride + t] = s;
+        const C s = wsum(diff[k]);
+        if(lane == 0) P.partials[k * P.partial_stride + t] = static_cast<double>(s);
       }
     }
   }

@@ -178,36 +178,39 @@ __device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* v, int64
   }
 }
 
-// block sum of the per-thread residual contributions into partials[k*stride + slot].
-// The warp level runs in the arithmetic type C (FP32 storages keep it off the
-// narrow FP64 pipe); warp sums and everything after them are FP64.
+// warp sum of the per-thread residual contributions into
+// partials[k*stride + slot], one slot per warp.  The sum runs in the
+// arithmetic type C (FP32 storages stay off the narrow FP64 pipe) and needs
+// no barrier; every later level is FP64.  All 32 lanes must arrive.
 template <int NV, class C>
-__device__ __forceinline__ void block_partials(const C* diff, double* partials, int64_t stride, int64_t slot) {
-  __shared__ double red[NV][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+__device__ __forceinline__ void warp_partials(const C* diff, double* partials, int64_t stride, int64_t slot) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for(int k = 0; k < NV; ++k) {
     const C s = warp_sum(diff[k]);
-    if(lane == 0) red[k][wid] = static_cast<double>(s);
+    if(lane == 0) partials[k * stride + slot] = static_cast<double>(s);
   }
-  __syncthreads();
-  if(wid == 0) {
+}
+
+// The previous moments are read at the top of the kernel (prefetch_moments),
+// together with the populations, so the residual adds no second round trip
+// to memory; moments_io writes the new ones and forms |new - previous|.
+template <class C, int MOM, int NV>
+__device__ __forceinline__ void prefetch_moments(const BoxParams& P, int64_t cell, C* prev) {
+  if constexpr(MOM == 2) {
+    const C* M = static_cast<const C*>(P.mom);
 #pragma unroll
-    for(int k = 0; k < NV; ++k) {
-      double s = lane < nw ? red[k][lane] : 0.0;
-      s        = warp_sum(s);
-      if(lane == 0) partials[k * stride + slot] = s;
-    }
+    for(int k = 0; k < NV; ++k) prev[k] = M[k * P.ncells + cell];
   }
 }
 
 template <int LAT, int EQ, class C, int MOM, int NV>
-__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, C* diff) {
+__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, const C* prev, C* diff) {
   if constexpr(MOM != 0) {
     C* M = static_cast<C*>(P.mom);
 #pragma unroll
     for(int k = 0; k < NV; ++k) {
-      if constexpr(MOM == 2) diff[k] = fabs(mom[k] - M[k * P.ncells + cell]);
+      if constexpr(MOM == 2) diff[k] = fabs(mom[k] - prev[k]);
       M[k * P.ncells + cell] = mom[k];
     }
   }
@@ -252,9 +255,10 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
 
   if(work) {
     C f[Q];
-    C mom[NV];
+    C mom[NV], prev[NV];
 #pragma unroll
     for(int k = 0; k < NV; ++k) mom[k] = 0;
+    prefetch_moments<C, MOM, NV>(P, cell, prev);
     const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     if(emit) {
       emit_equilibrium<LAT, EQ, C>(P, f, cell);
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
       }
       collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
     }
-    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
+    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
     if constexpr(!ODD) {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   }
   if constexpr(MOM == 2) {
     const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
-    block_partials<NV>(diff, P.partials, P.partial_stride, b);
+    warp_partials<NV>(diff, P.partials, P.partial_stride, b * (blockDim.x >> 5) + (threadIdx.x >> 5));
   }
 }
 
@@ -356,9 +360,10 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
     const uint8_t type = P.flags[cell] & TYPE_MASK;
     T*            A    = static_cast<T*>(P.pop);
     C             f[Q];
-    C             mom[NV];
+    C             mom[NV], prev[NV];
 #pragma unroll
     for(int k = 0; k < NV; ++k) mom[k] = 0;
+    prefetch_moments<C, MOM, NV>(P, cell, prev);
     if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
       emit_equilibrium<LAT, EQ, C>(P, f, cell);
     } else {
@@ -369,14 +374,14 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
       });
       collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
     }
-    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, diff);
+    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
       const int32_t d = dst[q * n + i];
       if(d >= 0) A[d] = S::store(corr_dst ? f[q] + static_cast<C>(corr_dst[q * n + i]) : f[q]);
     });
   }
-  if constexpr(MOM == 2) block_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x);
+  if constexpr(MOM == 2) warp_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
 }
 
 // outlet ghost fill, run before every step: for each outlet cell and each
@@ -618,7 +623,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p);
   }
   if(ev0) cudaEventRecord(ev0, s);
-  const int64_t nbulk = static_cast<int64_t>(g.x) * g.y * g.z;
+  const int64_t nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel
   const unsigned nbb  = static_cast<unsigned>((b->n_bnd + 127) / 128);
   if(odd) {
     if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
@@ -629,7 +634,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
       else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
       else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
     }
-    if(mom == 2) b->res_slots = nbulk + nbb;
+    if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
     if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
@@ -1035,7 +1040,10 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   if(e == cudaSuccess) e = cudaMalloc(&b->mom, csize * b->nvar * ncells);
   if(e == cudaSuccess) e = cudaMemset(b->mom, 0, csize * b->nvar * ncells);
   // partials for the largest launch (smallest block size considered by the tuner)
-  const int64_t maxblocks = static_cast<int64_t>((desc->nx + 63) / 64) * desc->ny * desc->nz + (b->n_bnd + 127) / 128;
+  // residual slots: one per warp of the largest launch over the tuner's block sizes
+  int64_t maxrow = 0;
+  for(int t : kTunerBlocks) maxrow = std::max<int64_t>(maxrow, static_cast<int64_t>((desc->nx + t - 1) / t) * (t / 32));
+  const int64_t maxblocks = maxrow * desc->ny * desc->nz + static_cast<int64_t>((b->n_bnd + 127) / 128) * 4;
   if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4 + kMidBlocks * 4));
   b->partials_mm      = b->partials + maxblocks * 4;
   b->partials_mid     = b->partials_mm + 304 * 4;
@@ -1076,7 +1084,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   // autotune the block size on the (not yet initialised) state
   {
     float best = 1e30f;
-    for(int tpb : {64, 128, 256}) {
+    for(int tpb : kTunerBlocks) {
       if(tpb > 2 * desc->nx && tpb > 64) continue;
       const float ms = time_pair(b, tpb, stream);
       if(ms < best) {

@@ -16,6 +16,8 @@ namespace lbm {
 
 // blocks of the first level of the residual reduction (two per SM on 152 SMs)
 constexpr int kMidBlocks = 304;
+// block sizes the step autotuner tries
+constexpr int kTunerBlocks[3] = {64, 128, 256};
 
 // Everything a box kernel needs, passed by value (kernel parameter space).
 struct BoxParams {
