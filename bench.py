@@ -266,6 +266,7 @@ def main():
     achieved = B_PER_CELL[args.storage] * cells / (kernel_avg_ms / 1e3) / 1e9
     _, u_head = s.moments()
     tpb = s.threads_per_block()
+    bulk_kernel = s.kernel()
     s.close()
 
     # the plain FP64 method and the other storages, same steps from the same start
@@ -333,9 +334,11 @@ def main():
         "config": {"workload": "D3Q19 flow past a sphere 512x256x256, r=24 at (128,128,128), eq. inlet u=0.05, zero-gradient outlet, "
                                "free-slip sides", "tau": case["tau"], "storage": args.storage, "cells": cells,
                    "bytes_per_cell": B_PER_CELL[args.storage], "l2": "state larger than L2 (no flush needed)",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "threads_per_block": tpb},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "threads_per_block": tpb,
+                   "bulk_kernel": bulk_kernel},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "k_box_step (AA step)", "kernel_avg_ms": kernel_avg_ms},
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
+                     "kernel_avg_ms": kernel_avg_ms},
         "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + args.steps},
         "variants": variants,
         "gpu_launches": int(launches * (2 if case["faces"][1] == "open" else 1)),

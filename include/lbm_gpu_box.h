@@ -84,9 +84,16 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
  * rho (or phi for Poisson) and ux, uy, uz (NULL to skip). */
 int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, double* uz);
 
-/* Launch configuration chosen by the autotuner (threads per block) and a
- * request to re-run it. */
+/* Threads per block the autotuner chose for the per-thread step kernel. */
 int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
+/* Bulk step kernel of a box context: LBM_BOX_KERNEL_THREAD (one global load
+ * per population and thread) or LBM_BOX_KERNEL_STAGED (each CTA stages whole
+ * rows in shared memory with bulk copies); lbm_gpu_create_box picks the faster
+ * by timing both.  Both give bit-identical results.  kernel < 0 only queries.
+ * LBM_ERR_UNSUPPORTED when the box does not qualify for staging (nx times the
+ * storage size must be a multiple of 16 bytes). */
+typedef enum lbm_box_kernel { LBM_BOX_KERNEL_THREAD = 0, LBM_BOX_KERNEL_STAGED = 1 } lbm_box_kernel;
+int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected);
 
 /* Run nsteps exactly as lbm_gpu_step does, but with a CUDA event pair around
  * every launch of the step kernel on the context's stream: total_ms is the

@@ -27,6 +27,7 @@ UNITS = {
     "table_engine.cu": ["-fmad=false"],
     "reduce.cu": [],
     "box.cu": [],
+    "box_tma.cu": [],
     "capi.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],

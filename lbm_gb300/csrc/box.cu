@@ -35,186 +35,12 @@
 #include <vector>
 
 #include "box.h"
+#include "box_device.cuh"
 #include "lattice.cuh"
-#include "step_common.cuh"
 #include "step_common.cuh"
 
 namespace lbm {
 namespace {
-
-constexpr uint8_t TYPE_MASK  = 0x07;
-constexpr uint8_t NEAR_SOLID = 0x08;  // set by the engine: a neighbour is solid
-// ---- link resolution ---------------------------------------------------------
-// mirror of direction q in the axes of `mask` (free-slip reflection)
-template <int LAT>
-__device__ __forceinline__ int mirror(int q, int mask) {
-  using L = Lattice<LAT>;
-  int c[3] = {L::c(q, 0), L::c(q, 1), L::c(q, 2)};
-#pragma unroll
-  for(int a = 0; a < 3; ++a)
-    if(mask & (1 << a)) c[a] = -c[a];
-#pragma unroll
-  for(int k = 0; k < L::Q; ++k)
-    if(L::c(k, 0) == c[0] && L::c(k, 1) == c[1] && L::c(k, 2) == c[2]) return k;
-  return q;
-}
-
-enum LinkKind { LINK_CELL = 0, LINK_BOUNCE = 1, LINK_OPEN = 2 };
-
-struct Link {
-  int     kind;
-  int64_t cell;  // LINK_CELL: cell to read / write
-  int     q;     // LINK_CELL: direction of the population at that cell
-  double  corr;  // LINK_BOUNCE: moving-wall momentum added to the arriving population
-};
-
-// Resolve the cell reached from (x,y,z) by displacement sign*c_q, through
-// the box faces.  sign=-1: source of the population arriving at (x,y,z) in
-// direction q; sign=+1: destination of the population leaving it.
-// `arrive` is the direction of the population that arrives at (x,y,z) when the
-// link bounces back (q for the pull side, opp(q) for the push side).
-template <int LAT>
-__device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z, int q, int sign, int arrive) {
-  using L       = Lattice<LAT>;
-  const int n[3] = {P.nx, P.ny, P.nz};
-  int       p[3] = {x, y, z};
-  int       s[3];
-  int       mask = 0;
-  bool      bb = false, open = false;
-  double    corr = 0.0;
-#pragma unroll
-  for(int a = 0; a < L::D; ++a) {
-    s[a] = p[a] + sign * L::c(q, a);
-    if(s[a] < 0 || s[a] >= n[a]) {
-      const int face = s[a] < 0 ? 2 * a : 2 * a + 1;
-      const int ft   = P.face[face];
-      if(ft == LBM_FACE_PERIODIC) {
-        s[a] = s[a] < 0 ? s[a] + n[a] : s[a] - n[a];
-      } else if(ft == LBM_FACE_FREESLIP) {
-        s[a] = p[a];
-        mask |= 1 << a;
-      } else if(ft == LBM_FACE_OPEN) {
-        open = true;
-      } else {
-        bb = true;
-        double cu = 0;
-#pragma unroll
-        for(int d = 0; d < L::D; ++d) cu += static_cast<double>(L::c(arrive, d)) * P.wall_u[face][d];
-        // 2 w (c.u_w) / c_s^2 with rho_w = 1, in state units S (delta f) / w
-        corr += 6.0 * STATE_SCALE * cu;
-      }
-    }
-  }
-#pragma unroll
-  for(int a = L::D; a < 3; ++a) s[a] = 0;
-  if(open) return Link{LINK_OPEN, 0, q, 0.0};
-  if(bb) return Link{LINK_BOUNCE, 0, q, corr};
-  const int64_t cell = s[0] + static_cast<int64_t>(P.nx) * (s[1] + static_cast<int64_t>(P.ny) * s[2]);
-  if((P.flags[cell] & TYPE_MASK) == LBM_CELL_SOLID) return Link{LINK_BOUNCE, 0, q, 0.0};
-  return Link{LINK_CELL, cell, mask ? mirror<LAT>(q, mask) : q, 0.0};
-}
-
-template <int LAT>
-__device__ __forceinline__ int64_t offset(const BoxParams& P, int q) {
-  using L = Lattice<LAT>;
-  return L::c(q, 0) + static_cast<int64_t>(P.nx) * (L::c(q, 1) + static_cast<int64_t>(P.ny) * L::c(q, 2));
-}
-
-template <int LAT>
-__device__ __forceinline__ bool interior(const BoxParams& P, int x, int y, int z) {
-  using L = Lattice<LAT>;
-  bool in = x > 0 && x < P.nx - 1;
-  if(L::D > 1) in = in && y > 0 && y < P.ny - 1;
-  if(L::D > 2) in = in && z > 0 && z < P.nz - 1;
-  return in;
-}
-
-// outlet ghost: value of direction q (c_qx = -1) for the outlet cell (y,z)
-__device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y, int z) {
-  return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
-}
-
-template <int LAT, int EQ, class C>
-__device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
-  if constexpr(EQ == LBM_NAVIER_STOKES) {
-    C F[3];
-    F[0] = prm<C>(P.force[0], P.force_f[0]);
-    F[1] = prm<C>(P.force[1], P.force_f[1]);
-    F[2] = prm<C>(P.force[2], P.force_f[2]);
-    collide_ns<LAT, C>(prm<C>(P.omega, P.omega_f), P.has_force != 0, F, v, mom_out);
-  } else {
-    collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
-                            mom_out);
-  }
-}
-
-// state emitted by inlet / Dirichlet cells
-template <int LAT, int EQ, class C>
-__device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* v, int64_t cell) {
-  using L         = Lattice<LAT>;
-  constexpr int Q = L::Q, D = L::D;
-  if constexpr(EQ == LBM_NAVIER_STOKES) {
-    const C rho = prm<C>(P.inlet_rho, P.inlet_rho_f);
-    C       ui[3];
-    static_for<D>([&](auto dc) { ui[decltype(dc)::value] = prm<C>(P.inlet_u[decltype(dc)::value], P.inlet_u_f[decltype(dc)::value]); });
-    C usq = 0;
-    static_for<D>([&](auto dc) { usq += ui[decltype(dc)::value] * ui[decltype(dc)::value]; });
-    static_for<Q>([&](auto qc) {
-      constexpr int q  = decltype(qc)::value;
-      C             cu = 0;
-      static_for<D>([&](auto dc) {
-        constexpr int d = decltype(dc)::value;
-        cu += static_cast<C>(L::c(q, d)) * ui[d];
-      });
-      const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
-      v[q]         = static_cast<C>(STATE_SCALE) * ((rho - C(1)) + rho * poly);
-    });
-  } else {
-    const C phi = P.dirichlet ? static_cast<C>(P.dirichlet[cell]) : C(0);
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      v[q]            = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
-    });
-  }
-}
-
-// warp sum of the per-thread residual contributions into
-// partials[k*stride + slot], one slot per warp.  The sum runs in the
-// arithmetic type C (FP32 storages stay off the narrow FP64 pipe) and needs
-// no barrier; every later level is FP64.  All 32 lanes must arrive.
-template <int NV, class C>
-__device__ __forceinline__ void warp_partials(const C* diff, double* partials, int64_t stride, int64_t slot) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for(int k = 0; k < NV; ++k) {
-    const C s = warp_sum(diff[k]);
-    if(lane == 0) partials[k * stride + slot] = static_cast<double>(s);
-  }
-}
-
-// The previous moments are read at the top of the kernel (prefetch_moments),
-// together with the populations, so the residual adds no second round trip
-// to memory; moments_io writes the new ones and forms |new - previous|.
-template <class C, int MOM, int NV>
-__device__ __forceinline__ void prefetch_moments(const BoxParams& P, int64_t cell, C* prev) {
-  if constexpr(MOM == 2) {
-    const C* M = static_cast<const C*>(P.mom);
-#pragma unroll
-    for(int k = 0; k < NV; ++k) prev[k] = M[k * P.ncells + cell];
-  }
-}
-
-template <int LAT, int EQ, class C, int MOM, int NV>
-__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, const C* prev, C* diff) {
-  if constexpr(MOM != 0) {
-    C* M = static_cast<C*>(P.mom);
-#pragma unroll
-    for(int k = 0; k < NV; ++k) {
-      if constexpr(MOM == 2) diff[k] = fabs(mom[k] - prev[k]);
-      M[k * P.ncells + cell] = mom[k];
-    }
-  }
-}
 
 // ---- the step kernels ----------------------------------------------------------
 // k_box_bulk: 3D grid over the box, one thread per cell.
@@ -623,10 +449,15 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p);
   }
   if(ev0) cudaEventRecord(ev0, s);
-  const int64_t nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel
-  const unsigned nbb  = static_cast<unsigned>((b->n_bnd + 127) / 128);
+  int64_t        nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel
+  const unsigned nbb   = static_cast<unsigned>((b->n_bnd + 127) / 128);
+  if(b->use_tma) {
+    const cudaError_t e = box_tma_bulk(b, odd, mom, s, &nbulk);
+    if(e != cudaSuccess) return e;
+  }
   if(odd) {
-    if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
+    if(b->use_tma) {
+    } else if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
     if(nbb) {
@@ -636,7 +467,8 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     }
     if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
-    if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
+    if(b->use_tma) {
+    } else if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
     if(mom == 2) b->res_slots = nbulk;
@@ -699,6 +531,20 @@ bool ensure_staging(BoxState* b) {
 int cerr(std::string& err, cudaError_t e, const char* what) {
   err = std::string(what) + ": " + cudaGetErrorString(e);
   return LBM_ERR_CUDA;
+}
+
+// a staged kernel that gave up waiting for its copies leaves a flag behind
+int check_wait_flag(BoxState* b, std::string& err) {
+  if(!b->use_tma) return LBM_OK;
+  int         flag = 0;
+  cudaError_t e    = cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if(e != cudaSuccess) return cerr(err, e, "wait flag");
+  if(flag) {
+    cudaMemset(b->d_err, 0, sizeof(int));
+    err = "staged step kernel: a bulk-copy wait timed out (state of this step is invalid)";
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
 }
 
 void drop_graphs(BoxState* b) {
@@ -781,7 +627,7 @@ int box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
   }
   cudaError_t e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return cerr(err, e, "step sync");
-  return LBM_OK;
+  return check_wait_flag(b, err);
 }
 
 int box_residual(BoxState* b, double* r, cudaStream_t s, std::string& err) {
@@ -871,6 +717,7 @@ void box_destroy(BoxState* b) {
   cudaFree(b->link_dst);
   cudaFree(b->corr_src);
   cudaFree(b->corr_dst);
+  cudaFree(b->d_err);
   delete b;
 }
 
@@ -1049,6 +896,8 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   b->partials_mid     = b->partials_mm + 304 * 4;
   p.partial_stride    = maxblocks;
   if(e == cudaSuccess) e = cudaMalloc(&b->out, sizeof(double) * 8);
+  if(e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(int));
+  if(e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(int));
   p.flags     = b->flags;
   p.dirichlet = b->dirichlet;
   p.pop       = b->pop;
@@ -1091,6 +940,15 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
         best         = ms;
         b->tuned_tpb = tpb;
       }
+    }
+    // the bulk-copy staged bulk kernel, where the box allows it
+    if(box_tma_supported(b)) {
+      b->use_tma     = 1;
+      const float ms = time_pair(b, b->tuned_tpb, stream);
+      int         flag = 0;
+      cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+      b->use_tma = (ms < best && flag == 0) ? 1 : 0;
+      cudaMemset(b->d_err, 0, sizeof(int));
     }
     cudaMemsetAsync(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1), stream);
     if(cudaStreamSynchronize(stream) != cudaSuccess) {
@@ -1178,6 +1036,11 @@ int lbm_gpu_box_profile_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* total_ms
     lbm_internal_set_error(ctx, std::string("profile steps: ") + cudaGetErrorString(e));
     return LBM_ERR_CUDA;
   }
+  std::string werr;
+  if(check_wait_flag(b, werr) != LBM_OK) {
+    lbm_internal_set_error(ctx, werr);
+    return LBM_ERR_CUDA;
+  }
   if(total_ms) *total_ms = tot;
   if(kernel_ms) *kernel_ms = ker;
   if(launches) *launches = nsteps;
@@ -1188,6 +1051,22 @@ int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block) {
   BoxState* b = lbm_internal_box(ctx);
   if(!b) return LBM_ERR_INVALID;
   if(threads_per_block) *threads_per_block = b->tuned_tpb;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b || kernel > LBM_BOX_KERNEL_STAGED) return LBM_ERR_INVALID;
+  if(kernel == LBM_BOX_KERNEL_STAGED && !box_tma_supported(b)) {
+    lbm_internal_set_error(ctx, "box does not qualify for the staged kernel (rows must be 16-byte multiples)");
+    return LBM_ERR_UNSUPPORTED;
+  }
+  if(kernel >= 0 && kernel != b->use_tma) {
+    cudaStreamSynchronize(lbm_internal_stream(ctx));
+    drop_graphs(b);
+    b->use_tma = kernel;
+  }
+  if(selected) *selected = b->use_tma;
   return LBM_OK;
 }
 

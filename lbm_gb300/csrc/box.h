@@ -72,6 +72,8 @@ struct BoxState {
   double*      corr_src  = nullptr;  // moving-wall terms (allocated only when a wall moves)
   double*      corr_dst  = nullptr;
   int64_t      res_slots = 0;        // partial slots written by the last residual step
+  int          use_tma   = 0;        // bulk kernel: 0 per-thread loads, 1 bulk-copy staged (box_tma.cu)
+  int*         d_err     = nullptr;  // set by a staged kernel whose bounded wait ran out
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
 };
 
@@ -83,6 +85,10 @@ int         box_set_populations(BoxState* b, const double* f, cudaStream_t s, st
 int         box_mass_momentum(BoxState* b, double* out, cudaStream_t s, std::string& err);
 int         box_info(const BoxState* b, int64_t* ncells, int32_t* q, int32_t* nvar);
 void        box_destroy(BoxState* b);
+// bulk-copy staged bulk kernel (box_tma.cu): whether the box qualifies, and
+// the launch; *slots = residual partial slots the launch writes
+bool        box_tma_supported(const BoxState* b);
+cudaError_t box_tma_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots);
 
 }  // namespace lbm
 

@@ -1,0 +1,191 @@
+// Device helpers of the dense-box engine shared by its step kernels
+// (box.cu: per-thread kernels; box_tma.cu: bulk-copy staged kernels): link
+// resolution through the faces, collision dispatch, inlet / Dirichlet
+// emission, and the residual bookkeeping of the moment-recording steps.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "box.h"
+#include "lattice.cuh"
+#include "step_common.cuh"
+
+namespace lbm {
+
+constexpr uint8_t TYPE_MASK  = 0x07;
+constexpr uint8_t NEAR_SOLID = 0x08;  // set by the engine: a neighbour is solid
+// ---- link resolution ---------------------------------------------------------
+// mirror of direction q in the axes of `mask` (free-slip reflection)
+template <int LAT>
+__device__ __forceinline__ int mirror(int q, int mask) {
+  using L = Lattice<LAT>;
+  int c[3] = {L::c(q, 0), L::c(q, 1), L::c(q, 2)};
+#pragma unroll
+  for(int a = 0; a < 3; ++a)
+    if(mask & (1 << a)) c[a] = -c[a];
+#pragma unroll
+  for(int k = 0; k < L::Q; ++k)
+    if(L::c(k, 0) == c[0] && L::c(k, 1) == c[1] && L::c(k, 2) == c[2]) return k;
+  return q;
+}
+
+enum LinkKind { LINK_CELL = 0, LINK_BOUNCE = 1, LINK_OPEN = 2 };
+
+struct Link {
+  int     kind;
+  int64_t cell;  // LINK_CELL: cell to read / write
+  int     q;     // LINK_CELL: direction of the population at that cell
+  double  corr;  // LINK_BOUNCE: moving-wall momentum added to the arriving population
+};
+
+// Resolve the cell reached from (x,y,z) by displacement sign*c_q, through
+// the box faces.  sign=-1: source of the population arriving at (x,y,z) in
+// direction q; sign=+1: destination of the population leaving it.
+// `arrive` is the direction of the population that arrives at (x,y,z) when the
+// link bounces back (q for the pull side, opp(q) for the push side).
+template <int LAT>
+__device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z, int q, int sign, int arrive) {
+  using L       = Lattice<LAT>;
+  const int n[3] = {P.nx, P.ny, P.nz};
+  int       p[3] = {x, y, z};
+  int       s[3];
+  int       mask = 0;
+  bool      bb = false, open = false;
+  double    corr = 0.0;
+#pragma unroll
+  for(int a = 0; a < L::D; ++a) {
+    s[a] = p[a] + sign * L::c(q, a);
+    if(s[a] < 0 || s[a] >= n[a]) {
+      const int face = s[a] < 0 ? 2 * a : 2 * a + 1;
+      const int ft   = P.face[face];
+      if(ft == LBM_FACE_PERIODIC) {
+        s[a] = s[a] < 0 ? s[a] + n[a] : s[a] - n[a];
+      } else if(ft == LBM_FACE_FREESLIP) {
+        s[a] = p[a];
+        mask |= 1 << a;
+      } else if(ft == LBM_FACE_OPEN) {
+        open = true;
+      } else {
+        bb = true;
+        double cu = 0;
+#pragma unroll
+        for(int d = 0; d < L::D; ++d) cu += static_cast<double>(L::c(arrive, d)) * P.wall_u[face][d];
+        // 2 w (c.u_w) / c_s^2 with rho_w = 1, in state units S (delta f) / w
+        corr += 6.0 * STATE_SCALE * cu;
+      }
+    }
+  }
+#pragma unroll
+  for(int a = L::D; a < 3; ++a) s[a] = 0;
+  if(open) return Link{LINK_OPEN, 0, q, 0.0};
+  if(bb) return Link{LINK_BOUNCE, 0, q, corr};
+  const int64_t cell = s[0] + static_cast<int64_t>(P.nx) * (s[1] + static_cast<int64_t>(P.ny) * s[2]);
+  if((P.flags[cell] & TYPE_MASK) == LBM_CELL_SOLID) return Link{LINK_BOUNCE, 0, q, 0.0};
+  return Link{LINK_CELL, cell, mask ? mirror<LAT>(q, mask) : q, 0.0};
+}
+
+template <int LAT>
+__device__ __forceinline__ int64_t offset(const BoxParams& P, int q) {
+  using L = Lattice<LAT>;
+  return L::c(q, 0) + static_cast<int64_t>(P.nx) * (L::c(q, 1) + static_cast<int64_t>(P.ny) * L::c(q, 2));
+}
+
+template <int LAT>
+__device__ __forceinline__ bool interior(const BoxParams& P, int x, int y, int z) {
+  using L = Lattice<LAT>;
+  bool in = x > 0 && x < P.nx - 1;
+  if(L::D > 1) in = in && y > 0 && y < P.ny - 1;
+  if(L::D > 2) in = in && z > 0 && z < P.nz - 1;
+  return in;
+}
+
+// outlet ghost: value of direction q (c_qx = -1) for the outlet cell (y,z)
+__device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y, int z) {
+  return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
+}
+
+template <int LAT, int EQ, class C>
+__device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    C F[3];
+    F[0] = prm<C>(P.force[0], P.force_f[0]);
+    F[1] = prm<C>(P.force[1], P.force_f[1]);
+    F[2] = prm<C>(P.force[2], P.force_f[2]);
+    collide_ns<LAT, C>(prm<C>(P.omega, P.omega_f), P.has_force != 0, F, v, mom_out);
+  } else {
+    collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
+                            mom_out);
+  }
+}
+
+// state emitted by inlet / Dirichlet cells
+template <int LAT, int EQ, class C>
+__device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* v, int64_t cell) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    const C rho = prm<C>(P.inlet_rho, P.inlet_rho_f);
+    C       ui[3];
+    static_for<D>([&](auto dc) { ui[decltype(dc)::value] = prm<C>(P.inlet_u[decltype(dc)::value], P.inlet_u_f[decltype(dc)::value]); });
+    C usq = 0;
+    static_for<D>([&](auto dc) { usq += ui[decltype(dc)::value] * ui[decltype(dc)::value]; });
+    static_for<Q>([&](auto qc) {
+      constexpr int q  = decltype(qc)::value;
+      C             cu = 0;
+      static_for<D>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        cu += static_cast<C>(L::c(q, d)) * ui[d];
+      });
+      const C poly = C(3) * cu + C(4.5) * cu * cu - C(1.5) * usq;
+      v[q]         = static_cast<C>(STATE_SCALE) * ((rho - C(1)) + rho * poly);
+    });
+  } else {
+    const C phi = P.dirichlet ? static_cast<C>(P.dirichlet[cell]) : C(0);
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      v[q]            = q == Q - 1 ? static_cast<C>(L::w(Q - 1) - 1.0) * phi : static_cast<C>(L::w(q)) * phi;
+    });
+  }
+}
+
+// warp sum of the per-thread residual contributions into
+// partials[k*stride + slot], one slot per warp.  The sum runs in the
+// arithmetic type C (FP32 storages stay off the narrow FP64 pipe) and needs
+// no barrier; every later level is FP64.  All 32 lanes must arrive.
+template <int NV, class C>
+__device__ __forceinline__ void warp_partials(const C* diff, double* partials, int64_t stride, int64_t slot) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for(int k = 0; k < NV; ++k) {
+    const C s = warp_sum(diff[k]);
+    if(lane == 0) partials[k * stride + slot] = static_cast<double>(s);
+  }
+}
+
+// The previous moments are read at the top of the kernel (prefetch_moments),
+// together with the populations, so the residual adds no second round trip
+// to memory; moments_io writes the new ones and forms |new - previous|.
+template <class C, int MOM, int NV>
+__device__ __forceinline__ void prefetch_moments(const BoxParams& P, int64_t cell, C* prev) {
+  if constexpr(MOM == 2) {
+    const C* M = static_cast<const C*>(P.mom);
+#pragma unroll
+    for(int k = 0; k < NV; ++k) prev[k] = M[k * P.ncells + cell];
+  }
+}
+
+template <int LAT, int EQ, class C, int MOM, int NV>
+__device__ __forceinline__ void moments_io(const BoxParams& P, int64_t cell, const C* mom, const C* prev, C* diff) {
+  if constexpr(MOM != 0) {
+    C* M = static_cast<C*>(P.mom);
+#pragma unroll
+    for(int k = 0; k < NV; ++k) {
+      if constexpr(MOM == 2) diff[k] = fabs(mom[k] - prev[k]);
+      M[k * P.ncells + cell] = mom[k];
+    }
+  }
+}
+
+}  // namespace lbm

@@ -1,0 +1,321 @@
+// Dense-box step with bulk-copy (TMA) staging of the populations.
+//
+// The per-thread step kernel (box.cu) loads each population with its own
+// global load; in FP16 storage that is 2 bytes per load and per register, so
+// the bytes a warp can keep in flight are bounded by its registers and the
+// kernel stalls on memory latency well below HBM bandwidth.  Here a CTA walks
+// a list of row segments (SEG consecutive cells of one x-row) and, one
+// segment per pipeline stage, has one thread issue a 1D bulk copy
+// (cp.async.bulk, completion on an mbarrier) for every direction's row:
+//   even step: row (y, z) of plane q, x in [x0, x0 + SEG);
+//   odd step:  row (y - c_qy, z - c_qz) of plane opp(q), x in
+//              [x0 - H, x0 + SEG + H), H = 16 bytes of halo on either side
+//              so that the copy starts on a 16-byte boundary.
+// NST segments are in flight per CTA while the threads collide the current
+// one from shared memory and store the results straight to global memory
+// (even: A[opp q][x]; odd: A[q][x + c_q]), exactly the AA update of the
+// per-thread kernel.  Halo elements that belong to other segments may be
+// stale by the time they are copied; only the cell's own slots are used, and
+// each slot is read and written by the one thread that owns it.
+//
+// The odd step covers the cells of the per-thread bulk kernel (interior fluid
+// cells with no solid neighbour, on rows 1..n-2); the boundary-list kernel of
+// box.cu handles the rest afterwards.  Every mbarrier wait is bounded: after
+// kWaitLimitNs the CTA records an error flag, waits (bounded again) for its
+// own copies still in flight and returns; the host reports the flag.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "box.h"
+#include "box_device.cuh"
+#include "lattice.cuh"
+#include "step_common.cuh"
+
+namespace lbm {
+namespace {
+
+constexpr int      kSeg        = 256;          // cells per segment = threads per CTA
+constexpr uint64_t kWaitLimitNs = 500000000ull;  // 0.5 s per wait
+
+template <class T>
+constexpr int stages() {
+  return sizeof(T) >= 8 ? 2 : 4;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait for phase `parity` of the barrier, giving up after kWaitLimitNs
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  if(mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while(!mbar_try_wait(bar, parity))
+    if(global_ns() - t0 > kWaitLimitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src),
+               "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+struct SegList {
+  int     segs_per_row;  // ceil(nx / kSeg)
+  int     y0, nrows_y;   // rows covered: y in [y0, y0 + nrows_y)
+  int     z0;            // z in [z0, ...)
+  int64_t nseg;          // segments in the list
+  int*    err;           // set to 1 when a wait times out
+};
+
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+__global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
+  using L               = Lattice<LAT>;
+  using S               = Store<ST>;
+  using T               = typename S::T;
+  using C               = typename S::C;
+  constexpr int Q       = L::Q;
+  constexpr int NV      = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
+  constexpr int NST     = stages<T>();
+  constexpr int HALO    = ODD ? static_cast<int>(16 / sizeof(T)) : 0;
+  constexpr int ROW     = kSeg + 2 * HALO;  // staged elements per direction
+  constexpr int STAGE   = Q * ROW;          // staged elements per segment
+  extern __shared__ __align__(128) unsigned char smem[];
+  T*        buf = reinterpret_cast<T*>(smem);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);
+
+  const int     tid  = threadIdx.x;
+  const int64_t nloc = static_cast<int64_t>(blockIdx.x) < W.nseg ? (W.nseg - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  if(tid == 0) {
+#pragma unroll
+    for(int s = 0; s < NST; ++s) mbar_init(smem_u32(&bar[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+
+  T* const      A  = static_cast<T*>(P.pop);
+  const int     NA = static_cast<int>(P.nalloc);
+  const int     nx = P.nx, ny = P.ny;
+
+  auto coords = [&](int64_t i, int& x0, int& y, int& z) {
+    const int64_t s = blockIdx.x + i * gridDim.x;
+    x0              = static_cast<int>(s % W.segs_per_row) * kSeg;
+    const int64_t r = s / W.segs_per_row;
+    y               = W.y0 + static_cast<int>(r % W.nrows_y);
+    z               = W.z0 + static_cast<int>(r / W.nrows_y);
+  };
+  // thread 0: stage the rows of local segment i
+  auto issue = [&](int64_t i) {
+    int x0, y, z;
+    coords(i, x0, y, z);
+    const int      st    = static_cast<int>(i % NST);
+    const int      lo    = ODD ? max(x0 - HALO, 0) : x0;
+    const int      hi    = min(x0 + kSeg + HALO, nx);
+    const uint32_t bytes = static_cast<uint32_t>(hi - lo) * sizeof(T);
+    const uint32_t b     = smem_u32(&bar[st]);
+    mbar_expect_tx(b, bytes * Q);
+    T* const dst0 = buf + st * STAGE + (lo - (x0 - HALO));
+    static_for<Q>([&](auto qc) {
+      constexpr int q     = decltype(qc)::value;
+      constexpr int plane = ODD ? L::opp(q) : q;
+      const int     ys    = ODD ? y - L::c(q, 1) : y;
+      const int     zs    = ODD ? z - L::c(q, 2) : z;
+      const T*      src   = A + static_cast<int64_t>(plane) * NA + lo + static_cast<int64_t>(nx) * (ys + static_cast<int64_t>(ny) * zs);
+      bulk_g2s(smem_u32(dst0 + q * ROW), src, bytes, b);
+    });
+  };
+  // give up: flag the error and wait (bounded) for the copies still in flight
+  auto bail = [&](int64_t from) {
+    if(tid == 0) {
+      atomicExch(W.err, 1);
+      for(int64_t j = from; j < nloc && j < from + NST; ++j) mbar_wait_bounded(smem_u32(&bar[j % NST]), static_cast<uint32_t>((j / NST) & 1));
+    }
+  };
+
+  if(tid == 0)
+    for(int64_t i = 0; i < nloc && i < NST; ++i) issue(i);
+
+  for(int64_t i = 0; i < nloc; ++i) {
+    int x0, y, z;
+    coords(i, x0, y, z);
+    const int     st    = static_cast<int>(i % NST);
+    const int     x     = x0 + tid;
+    const bool    valid = x < nx;
+    const int     cell  = valid ? x + nx * (y + ny * z) : 0;
+    const uint8_t flag  = valid ? P.flags[cell] : LBM_CELL_SOLID;
+    const uint8_t type  = flag & TYPE_MASK;
+    bool          work;
+    if constexpr(ODD) work = type == LBM_CELL_FLUID && !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+    else work = type != LBM_CELL_SOLID;
+    const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+    C          mom[NV], prev[NV], diff[NV];
+#pragma unroll
+    for(int k = 0; k < NV; ++k) {
+      mom[k]  = C(0);
+      diff[k] = C(0);
+    }
+    if(work) prefetch_moments<C, MOM, NV>(P, cell, prev);
+
+    const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&bar[st]), static_cast<uint32_t>((i / NST) & 1)));
+    if(!ok) {
+      bail(i);
+      return;
+    }
+    C        f[Q];
+    const T* row = buf + st * STAGE + HALO + tid;
+    if(work && !emit)
+      static_for<Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        f[q]            = S::load(row[q * ROW - (ODD ? L::c(q, 0) : 0)]);
+      });
+    __syncthreads();  // the stage is free again
+    if(tid == 0 && i + NST < nloc) issue(i + NST);
+
+    if(work) {
+      if(emit) {
+        emit_equilibrium<LAT, EQ, C>(P, f, cell);
+      } else {
+        if constexpr(!ODD) {
+          if(type == LBM_CELL_OUTLET) {
+            static_for<Q>([&](auto qc) {
+              constexpr int q = decltype(qc)::value;
+              if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+            });
+          }
+        }
+        collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
+      }
+      moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
+      if constexpr(!ODD) {
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          A[L::opp(q) * NA + cell] = S::store(f[q]);
+        });
+      } else {
+        const int sy = nx, sz = nx * ny;
+        static_for<Q>([&](auto qc) {
+          constexpr int q   = decltype(qc)::value;
+          const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+          A[q * NA + cell + off] = S::store(f[q]);
+        });
+      }
+    }
+    if constexpr(MOM == 2) {
+      const int64_t s = blockIdx.x + i * gridDim.x;
+      warp_partials<NV>(diff, P.partials, P.partial_stride, s * (kSeg / 32) + (tid >> 5));
+    }
+  }
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+cudaError_t launch_one(BoxState* b, const SegList& W, cudaStream_t s) {
+  using T          = typename Store<ST>::T;
+  constexpr int NST = stages<T>();
+  constexpr int HALO = ODD ? static_cast<int>(16 / sizeof(T)) : 0;
+  const size_t smem = sizeof(T) * NST * Lattice<LAT>::Q * (kSeg + 2 * HALO) + sizeof(uint64_t) * NST;
+  auto         kern = k_box_tma<LAT, EQ, ST, ODD, MOM>;
+  // resident CTAs on the whole GPU, worked out once per instantiation
+  static int resident = 0;
+  if(resident == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if(e != cudaSuccess) return e;
+    int per_sm = 0;
+    e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSeg, smem);
+    if(e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    resident = std::max(per_sm, 1) * sms;
+  }
+  const int64_t grid = std::min<int64_t>(W.nseg, resident);
+  if(grid <= 0) return cudaSuccess;
+  kern<<<static_cast<unsigned>(grid), kSeg, smem, s>>>(b->p, W);
+  return cudaGetLastError();
+}
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_tma(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots) {
+  using L = Lattice<LAT>;
+  SegList W{};
+  W.segs_per_row = (b->p.nx + kSeg - 1) / kSeg;
+  W.err          = b->d_err;
+  if(odd) {
+    W.y0      = L::D > 1 ? 1 : 0;
+    W.nrows_y = L::D > 1 ? b->p.ny - 2 : b->p.ny;
+    W.z0      = L::D > 2 ? 1 : 0;
+    const int nz = L::D > 2 ? b->p.nz - 2 : b->p.nz;
+    W.nseg    = (W.nrows_y > 0 && nz > 0) ? static_cast<int64_t>(W.segs_per_row) * W.nrows_y * nz : 0;
+  } else {
+    W.y0      = 0;
+    W.nrows_y = b->p.ny;
+    W.z0      = 0;
+    W.nseg    = static_cast<int64_t>(W.segs_per_row) * b->p.ny * b->p.nz;
+  }
+  *slots = W.nseg * (kSeg / 32);
+  if(W.nseg == 0) return cudaSuccess;
+  if(odd) {
+    if(mom == 0) return launch_one<LAT, EQ, ST, true, 0>(b, W, s);
+    if(mom == 1) return launch_one<LAT, EQ, ST, true, 1>(b, W, s);
+    return launch_one<LAT, EQ, ST, true, 2>(b, W, s);
+  }
+  if(mom == 0) return launch_one<LAT, EQ, ST, false, 0>(b, W, s);
+  if(mom == 1) return launch_one<LAT, EQ, ST, false, 1>(b, W, s);
+  return launch_one<LAT, EQ, ST, false, 2>(b, W, s);
+}
+
+}  // namespace
+
+bool box_tma_supported(const BoxState* b) {
+  // every staged row must start on a 16-byte boundary: planes are padded to
+  // 128 cells, so rows are aligned when nx * sizeof(storage) is
+  if(!b->d_err) return false;
+  if((static_cast<size_t>(b->p.nx) * b->elem) % 16 != 0) return false;
+  if((static_cast<size_t>(b->p.nalloc) * b->elem) % 16 != 0) return false;
+  return true;
+}
+
+cudaError_t box_tma_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots) {
+  const int key = b->desc.lattice * 100 + b->desc.equation * 10 + b->desc.storage;
+  switch(key) {
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F64: return launch_tma<LBM_D2Q9, 0, LBM_STORE_F64>(b, odd, mom, s, slots);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return launch_tma<LBM_D2Q9, 0, LBM_STORE_F32>(b, odd, mom, s, slots);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return launch_tma<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, slots);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_tma<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, slots);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return launch_tma<LBM_D3Q19, 0, LBM_STORE_F64>(b, odd, mom, s, slots);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return launch_tma<LBM_D3Q19, 0, LBM_STORE_F32>(b, odd, mom, s, slots);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return launch_tma<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, slots);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_tma<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, slots);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return launch_tma<LBM_D3Q7, 1, LBM_STORE_F64>(b, odd, mom, s, slots);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return launch_tma<LBM_D3Q7, 1, LBM_STORE_F32>(b, odd, mom, s, slots);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace lbm

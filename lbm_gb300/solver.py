@@ -240,6 +240,16 @@ class BoxSolver:
         check(self._lib.lbm_gpu_box_autotune(self.ctx, C.byref(t)), self.ctx, "autotune")
         return t.value
 
+    KERNELS = {"thread": 0, "staged": 1}
+
+    def kernel(self, kind: Optional[str] = None) -> str:
+        """The bulk step kernel in use ("thread" or "staged"); with `kind`,
+        switch to it first (both give bit-identical results)."""
+        sel = C.c_int32()
+        check(self._lib.lbm_gpu_box_select_kernel(self.ctx, -1 if kind is None else self.KERNELS[kind], C.byref(sel)), self.ctx,
+              "select_kernel")
+        return "staged" if sel.value == 1 else "thread"
+
 
 # ---- the reference's run loop -------------------------------------------------
 
