@@ -185,6 +185,73 @@ def cavities_run(args):
                     "of": int(len(area))}}
 
 
+def poisson_run(args):
+    """D3Q7 Poisson-Boltzmann on 256^3 (seeded charged spheres, Debye length
+    and surface potentials by seed): device-timed steps in FP32 storage, the
+    FP32 solve to residual 1e-10 (FP64 residual reductions), and the FP32
+    potential against an FP64 run after the same 5,000 steps."""
+    from lbm_gb300 import cases
+    from lbm_gb300.solver import BoxSolver
+
+    c = cases.pb_spheres(256, seed=7)
+    kw = cases.box_kwargs(c)
+    hbm, peak_kind = peaks()
+    cells = 256 ** 3
+    out = {"metric": "MLUPS (D3Q7 Poisson-Boltzmann 256^3, FP32 storage)", "unit": "MLUPS", "dtype": "f32",
+           "config": {"workload": f"D3Q7 Poisson-Boltzmann 256^3, {len(c['spheres'])} spheres, Debye length {c['debye']:.2f}",
+                      "cells": cells, "bytes_per_cell": 2 * 7 * 4 + 1}}
+    g = BoxSolver(c["lattice"], c["shape"], c["omega"], "f32", pb_nonlinear=True, **kw)
+    g.initial_condition()
+    g.step(args.warmup)
+    tot, ker, n = g.profile_steps(args.steps)
+    out["value"] = cells * args.steps / (tot / 1e3) / 1e6
+    ach = (2 * 7 * 4 + 1) * cells / (ker / n / 1e3) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_kind": peak_kind}
+    g.initial_condition()
+    g.step(5000)
+    phi32, _ = g.moments()
+    t0 = time.perf_counter()
+    steps, res = g.run_to(1e-10, 1000, args.max_steps - 5000)
+    wall = time.perf_counter() - t0
+    out["solve_f32"] = {"steps": steps + 5000, "wall_s_after_5000": wall, "residual": float(np.max(res)), "converged": bool(np.max(res) < 1e-10)}
+    g.close()
+    h = BoxSolver(c["lattice"], c["shape"], c["omega"], "f64", pb_nonlinear=True, **kw)
+    h.initial_condition()
+    t0 = time.perf_counter()
+    h.step(5000)
+    out["f64_mlups"] = cells * 5000 / (time.perf_counter() - t0) / 1e6
+    phi64, _ = h.moments()
+    h.close()
+    out["phi_rel_l2_f32_vs_f64_at_5000"] = float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64))
+    return out
+
+
+def poiseuille_run(args):
+    """D2Q9 Guo-forced Poiseuille channel 256x64, plain FP64, 20,000 steps
+    (the state fits in L2): device-timed MLUPS and the deviation from the
+    analytic parabola."""
+    from lbm_gb300 import cases
+    from lbm_gb300.solver import BoxSolver
+
+    c = cases.poiseuille_guo()
+    g = BoxSolver(c["lattice"], c["shape"], c["omega"], "f64", **cases.box_kwargs(c))
+    g.initial_condition()
+    g.step(args.warmup)
+    tot, ker, n = g.profile_steps(200)
+    g.initial_condition()
+    t0 = time.perf_counter()
+    g.step(20000)
+    wall = time.perf_counter() - t0
+    _, u = g.moments()
+    ux = u[0].reshape(64, 256).mean(axis=1)
+    exact = cases.poiseuille_profile(64, c["tau"], c["g"])
+    g.close()
+    return {"metric": "MLUPS (D2Q9 Guo Poiseuille 256x64, FP64)", "unit": "MLUPS", "dtype": "f64",
+            "value": 256 * 64 * 20000 / wall / 1e6, "device_timed_mlups": 256 * 64 * 200 / (tot / 1e3) / 1e6,
+            "config": {"workload": "D2Q9 Guo Poiseuille 256x64, tau 0.8, g 1e-6, 20,000 steps", "cells": 256 * 64},
+            "analytic_max_rel_dev_after_20000": float(np.abs(ux - exact).max() / exact.max())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -193,8 +260,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities"],
-                    help="cavities: the batched-cavity engine instead of the headline sphere workload")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille"],
+                    help="the headline sphere workload, or one of the other configurations (one JSON line each)")
+    ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann solves")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
@@ -212,9 +280,10 @@ def main():
         return
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "cavities":
+    if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
-            print(json.dumps(cavities_run(args)))
+            fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run}[args.workload]
+            print(json.dumps(fn(args)))
         return
 
     rank = int(os.environ.get("RANK", "0"))

@@ -31,6 +31,7 @@ UNITS = {
     "capi.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],
+    "unet.cu": [],
 }
 
 

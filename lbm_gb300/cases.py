@@ -95,6 +95,69 @@ def cavities(count: int = 2048, seed: int = 11, lid: float = 0.1, nmin: int = 32
     return dict(sides=sides.astype(np.int32), re=re, tau=tau, lid=lid)
 
 
+def cylinder_channel(seed: int, nx: int = 512, ny: int = 128, u_in: float = 0.05, re: float | None = None) -> Dict:
+    """D2Q9 channel for the learned warm start: 1-8 non-overlapping cylinders
+    of radius 6-20 cells at ny = 128, scaled with ny (solid where the cell
+    centre is inside), equilibrium
+    inlet u_in at x = 0, zero-gradient outlet at x = nx-1, bounce-back walls
+    at y = -1/2 and ny - 1/2.  Re = u_in * ny / nu is drawn uniformly from
+    [20, 200] (channel-height Reynolds number: the cylinder Reynolds numbers
+    then stay below the onset of shedding, so every case has a steady state);
+    `re` overrides the drawn value (cases stacked in one box share it)."""
+    rng = np.random.default_rng(seed)
+    count = int(rng.integers(1, 9))
+    re_drawn = float(rng.uniform(20.0, 200.0))
+    re = re_drawn if re is None else float(re)
+    cyl: List = []
+    tries = 0
+    while len(cyl) < count and tries < 10000:
+        tries += 1
+        r = float(rng.uniform(6.0, 20.0)) * ny / 128.0  # radii scale with the channel height
+        cx = float(rng.uniform(r + 0.1875 * ny, nx - r - 0.75 * ny))
+        cy = float(rng.uniform(r + 3.0, ny - r - 3.0))
+        if all((cx - x2) ** 2 + (cy - y2) ** 2 > (r + r2 + 3.0) ** 2 for x2, y2, r2 in cyl):
+            cyl.append((cx, cy, r))
+    y, x = np.meshgrid(np.arange(ny) + 0.5, np.arange(nx) + 0.5, indexing="ij")
+    flags = np.zeros((ny, nx), dtype=np.uint8)
+    for cx, cy, r in cyl:
+        flags[(x - cx) ** 2 + (y - cy) ** 2 < r * r] = SOLID
+    flags[:, 0] = INLET
+    flags[:, -1] = OUTLET
+    nu = u_in * ny / re
+    return dict(flags=flags, re=re, tau=3.0 * nu + 0.5, cylinders=cyl, u_in=u_in, shape=(nx, ny))
+
+
+def forced_channel(seed: int, nx: int = 512, ny: int = 128, u_ref: float = 0.08, re: float | None = None) -> Dict:
+    """The warm-start channel in its closed form: the cylinders of
+    cylinder_channel(seed), periodic in x, bounce-back walls at y = -1/2 and
+    ny - 1/2, driven by a Guo body force g.  Re = u_ref ny / nu with u_ref =
+    g ny^2 / (8 nu), the centre-line speed of the empty channel; Re is drawn
+    uniformly from [20, 200] (or given).  Mass is conserved exactly, so the
+    steady state is unique for the initial mass."""
+    c = cylinder_channel(seed, nx, ny, re=re)
+    flags = (c["flags"] == SOLID).astype(np.uint8) * SOLID
+    nu = u_ref * ny / c["re"]
+    return dict(flags=flags, re=c["re"], tau=3.0 * nu + 0.5, g=8.0 * nu * u_ref / (ny * ny), cylinders=c["cylinders"], u_ref=u_ref,
+                shape=(nx, ny))
+
+
+def stacked_forced(cases_: List[Dict]) -> Dict:
+    """Several forced channels with one Re as the z-slices of one D2Q9 box."""
+    nx, ny = cases_[0]["shape"]
+    flags = np.stack([c["flags"] for c in cases_]).reshape(-1)
+    return dict(lattice=D2Q9, shape=(nx, ny, len(cases_)), omega=1.0 / cases_[0]["tau"], flags=flags,
+                faces=("periodic", "periodic", "wall", "wall", "periodic", "periodic"), body_force=(cases_[0]["g"], 0.0, 0.0))
+
+
+def stacked_channels(cases_: List[Dict], tau: float) -> Dict:
+    """Several 2D channels as the z-slices of one D2Q9 box (the lattice has no
+    z links, so the slices evolve independently) sharing one relaxation time."""
+    nx, ny = cases_[0]["shape"]
+    flags = np.stack([c["flags"] for c in cases_]).reshape(-1)
+    return dict(lattice=D2Q9, shape=(nx, ny, len(cases_)), omega=1.0 / tau, flags=flags,
+                faces=("open", "open", "wall", "wall", "periodic", "periodic"), inlet_velocity=(cases_[0]["u_in"], 0.0, 0.0))
+
+
 def box_kwargs(case: Dict) -> Dict:
     """The BoxSolver / BoxOracle keyword arguments of a case."""
     keys = ("faces", "flags", "wall_velocity", "body_force", "inlet_velocity", "equation", "kappa_sq", "dirichlet")

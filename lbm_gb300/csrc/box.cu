@@ -769,7 +769,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
                   (lat == LBM_D3Q7 && eq == LBM_POISSON && (st == LBM_STORE_F64 || st == LBM_STORE_F32));
   if(!ok) return LBM_ERR_UNSUPPORTED;
   const int D = lat == LBM_D2Q9 ? 2 : 3;
-  if(desc->nx < 2 || desc->ny < 2 || (D == 3 && desc->nz < 2) || (D == 2 && desc->nz != 1)) return LBM_ERR_INVALID;
+  if(desc->nx < 2 || desc->ny < 2 || (D == 3 && desc->nz < 2) || desc->nz < 1) return LBM_ERR_INVALID;
   if(desc->ny > 65535 || desc->nz > 65535) return LBM_ERR_INVALID;
   if(!(desc->omega > 0.0 && desc->omega < 2.0)) return LBM_ERR_INVALID;
   for(int a = 0; a < D; ++a) {

@@ -78,7 +78,7 @@ __device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z,
     }
   }
 #pragma unroll
-  for(int a = L::D; a < 3; ++a) s[a] = 0;
+  for(int a = L::D; a < 3; ++a) s[a] = p[a];  // a 2D lattice on a stack of slices keeps its slice
   if(open) return Link{LINK_OPEN, 0, q, 0.0};
   if(bb) return Link{LINK_BOUNCE, 0, q, corr};
   const int64_t cell = s[0] + static_cast<int64_t>(P.nx) * (s[1] + static_cast<int64_t>(P.ny) * s[2]);

@@ -53,6 +53,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -86,16 +90,46 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                : "memory");
 }
 
-struct SegList {
-  int     segs_per_row;  // ceil(nx / kSeg)
-  int     y0, nrows_y;   // rows covered: y in [y0, y0 + nrows_y)
-  int     z0;            // z in [z0, ...)
-  int64_t nseg;          // segments in the list
-  int*    err;           // set to 1 when a wait times out
+// n / d for n < 2^31 by multiply-high (Granlund-Montgomery, round-up
+// multiplier): d fixed per launch, m and l set on the host
+struct FastDiv {
+  uint32_t d, m;
+  int      l;
 };
 
+inline FastDiv make_fastdiv(uint32_t d) {
+  int l = 0;
+  while((uint64_t(1) << l) < d) ++l;
+  const uint64_t m = ((uint64_t(1) << 32) * ((uint64_t(1) << l) - d)) / d + 1;
+  return FastDiv{d, static_cast<uint32_t>(m), l};
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) { return (__umulhi(n, f.m) + n) >> f.l; }
+
+struct SegList {
+  FastDiv spr;      // segments per row, ceil(nx / kSeg)
+  FastDiv nrows;    // rows per z-slab in the list
+  int     y0, z0;   // first row: y in [y0, y0 + nrows), z from z0
+  int     nseg;     // segments in the list
+  int*    err;      // set to 1 when a wait times out
+};
+
+constexpr int kConsumers = kSeg / 32;  // consumer warps; warp 0 issues the copies
+
+// Warp 0 is the producer: its lane 0 keeps NST segments of copies in flight,
+// re-using a stage once every consumer warp has released it (empty barrier).
+// Warps 1..kConsumers each own 32 cells of the segment: wait for the stage
+// (full barrier), read their populations, release the stage, collide, store.
+// No block-wide barrier after the set-up.
+// resident CTAs per SM the register budget aims at: three for the plain
+// FP32-arithmetic step, two where the moment bookkeeping or FP64 needs room
+template <int ST, int MOM>
+constexpr int min_ctas() {
+  return (ST == LBM_STORE_F64 || MOM != 0) ? 2 : 3;
+}
+
 template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
+__global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxParams P, SegList W) {
   using L               = Lattice<LAT>;
   using S               = Store<ST>;
   using T               = typename S::T;
@@ -107,65 +141,76 @@ __global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
   constexpr int ROW     = kSeg + 2 * HALO;  // staged elements per direction
   constexpr int STAGE   = Q * ROW;          // staged elements per segment
   extern __shared__ __align__(128) unsigned char smem[];
-  T*        buf = reinterpret_cast<T*>(smem);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);
+  T*        buf   = reinterpret_cast<T*>(smem);
+  uint64_t* full  = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);
+  uint64_t* empty = full + NST;
 
-  const int     tid  = threadIdx.x;
-  const int64_t nloc = static_cast<int64_t>(blockIdx.x) < W.nseg ? (W.nseg - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  if(tid == 0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G    = static_cast<int>(gridDim.x);
+  const int nloc = static_cast<int>(blockIdx.x) < W.nseg ? (W.nseg - 1 - static_cast<int>(blockIdx.x)) / G + 1 : 0;
+  if(threadIdx.x == 0) {
 #pragma unroll
-    for(int s = 0; s < NST; ++s) mbar_init(smem_u32(&bar[s]), 1);
+    for(int s = 0; s < NST; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), kConsumers);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
 
-  T* const      A  = static_cast<T*>(P.pop);
-  const int     NA = static_cast<int>(P.nalloc);
-  const int     nx = P.nx, ny = P.ny;
+  T* const  A  = static_cast<T*>(P.pop);
+  const int NA = static_cast<int>(P.nalloc);
+  const int nx = P.nx, ny = P.ny;
 
-  auto coords = [&](int64_t i, int& x0, int& y, int& z) {
-    const int64_t s = blockIdx.x + i * gridDim.x;
-    x0              = static_cast<int>(s % W.segs_per_row) * kSeg;
-    const int64_t r = s / W.segs_per_row;
-    y               = W.y0 + static_cast<int>(r % W.nrows_y);
-    z               = W.z0 + static_cast<int>(r / W.nrows_y);
+  auto coords = [&](int i, int& x0, int& y, int& z) {
+    const uint32_t s  = static_cast<uint32_t>(blockIdx.x) + static_cast<uint32_t>(i) * static_cast<uint32_t>(G);
+    const uint32_t r  = fdiv(s, W.spr);
+    const uint32_t zz = fdiv(r, W.nrows);
+    x0                = static_cast<int>(s - r * W.spr.d) * kSeg;
+    y                 = W.y0 + static_cast<int>(r - zz * W.nrows.d);
+    z                 = W.z0 + static_cast<int>(zz);
   };
-  // thread 0: stage the rows of local segment i
-  auto issue = [&](int64_t i) {
-    int x0, y, z;
-    coords(i, x0, y, z);
-    const int      st    = static_cast<int>(i % NST);
-    const int      lo    = ODD ? max(x0 - HALO, 0) : x0;
-    const int      hi    = min(x0 + kSeg + HALO, nx);
-    const uint32_t bytes = static_cast<uint32_t>(hi - lo) * sizeof(T);
-    const uint32_t b     = smem_u32(&bar[st]);
-    mbar_expect_tx(b, bytes * Q);
-    T* const dst0 = buf + st * STAGE + (lo - (x0 - HALO));
-    static_for<Q>([&](auto qc) {
-      constexpr int q     = decltype(qc)::value;
-      constexpr int plane = ODD ? L::opp(q) : q;
-      const int     ys    = ODD ? y - L::c(q, 1) : y;
-      const int     zs    = ODD ? z - L::c(q, 2) : z;
-      const T*      src   = A + static_cast<int64_t>(plane) * NA + lo + static_cast<int64_t>(nx) * (ys + static_cast<int64_t>(ny) * zs);
-      bulk_g2s(smem_u32(dst0 + q * ROW), src, bytes, b);
-    });
-  };
-  // give up: flag the error and wait (bounded) for the copies still in flight
-  auto bail = [&](int64_t from) {
-    if(tid == 0) {
-      atomicExch(W.err, 1);
-      for(int64_t j = from; j < nloc && j < from + NST; ++j) mbar_wait_bounded(smem_u32(&bar[j % NST]), static_cast<uint32_t>((j / NST) & 1));
+
+  if(warp == 0) {
+    // ---- producer ----
+    if(lane == 0) {
+      for(int i = 0; i < nloc; ++i) {
+        const int st = i % NST;
+        if(i >= NST && !mbar_wait_bounded(smem_u32(&empty[st]), static_cast<uint32_t>((i / NST - 1) & 1))) {
+          atomicExch(W.err, 1);
+          // copies already issued may still land: wait for them (bounded)
+          for(int j = i - NST; j < i; ++j)
+            if(j >= 0) mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1));
+          break;
+        }
+        int x0, y, z;
+        coords(i, x0, y, z);
+        const int      lo    = ODD ? max(x0 - HALO, 0) : x0;
+        const int      hi    = min(x0 + kSeg + HALO, nx);
+        const uint32_t bytes = static_cast<uint32_t>(hi - lo) * sizeof(T);
+        const uint32_t b     = smem_u32(&full[st]);
+        mbar_expect_tx(b, bytes * Q);
+        T* const dst0 = buf + st * STAGE + (lo - (x0 - HALO));
+        static_for<Q>([&](auto qc) {
+          constexpr int q     = decltype(qc)::value;
+          constexpr int plane = ODD ? L::opp(q) : q;
+          const int     ys    = ODD ? y - L::c(q, 1) : y;
+          const int     zs    = ODD ? z - L::c(q, 2) : z;
+          const T*      src   = A + plane * NA + lo + nx * (ys + ny * zs);
+          bulk_g2s(smem_u32(dst0 + q * ROW), src, bytes, b);
+        });
+      }
     }
-  };
+    return;
+  }
 
-  if(tid == 0)
-    for(int64_t i = 0; i < nloc && i < NST; ++i) issue(i);
-
-  for(int64_t i = 0; i < nloc; ++i) {
+  // ---- consumers ----
+  const int tid = threadIdx.x - 32;  // cell within the segment
+  for(int i = 0; i < nloc; ++i) {
     int x0, y, z;
     coords(i, x0, y, z);
-    const int     st    = static_cast<int>(i % NST);
+    const int     st    = i % NST;
     const int     x     = x0 + tid;
     const bool    valid = x < nx;
     const int     cell  = valid ? x + nx * (y + ny * z) : 0;
@@ -183,9 +228,10 @@ __global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
     }
     if(work) prefetch_moments<C, MOM, NV>(P, cell, prev);
 
-    const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&bar[st]), static_cast<uint32_t>((i / NST) & 1)));
+    // the wait result is made warp-uniform so the warp leaves together
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1)));
     if(!ok) {
-      bail(i);
+      if(lane == 0) atomicExch(W.err, 1);
       return;
     }
     C        f[Q];
@@ -195,8 +241,8 @@ __global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
         constexpr int q = decltype(qc)::value;
         f[q]            = S::load(row[q * ROW - (ODD ? L::c(q, 0) : 0)]);
       });
-    __syncthreads();  // the stage is free again
-    if(tid == 0 && i + NST < nloc) issue(i + NST);
+    __syncwarp();
+    if(lane == 0) mbar_arrive(smem_u32(&empty[st]));  // this warp is done with the stage
 
     if(work) {
       if(emit) {
@@ -228,8 +274,8 @@ __global__ void __launch_bounds__(kSeg) k_box_tma(BoxParams P, SegList W) {
       }
     }
     if constexpr(MOM == 2) {
-      const int64_t s = blockIdx.x + i * gridDim.x;
-      warp_partials<NV>(diff, P.partials, P.partial_stride, s * (kSeg / 32) + (tid >> 5));
+      const int64_t s = static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(i) * G;
+      warp_partials<NV>(diff, P.partials, P.partial_stride, s * kConsumers + (warp - 1));
     }
   }
 }
@@ -239,7 +285,7 @@ cudaError_t launch_one(BoxState* b, const SegList& W, cudaStream_t s) {
   using T          = typename Store<ST>::T;
   constexpr int NST = stages<T>();
   constexpr int HALO = ODD ? static_cast<int>(16 / sizeof(T)) : 0;
-  const size_t smem = sizeof(T) * NST * Lattice<LAT>::Q * (kSeg + 2 * HALO) + sizeof(uint64_t) * NST;
+  const size_t smem = sizeof(T) * NST * Lattice<LAT>::Q * (kSeg + 2 * HALO) + sizeof(uint64_t) * 2 * NST;
   auto         kern = k_box_tma<LAT, EQ, ST, ODD, MOM>;
   // resident CTAs on the whole GPU, worked out once per instantiation
   static int resident = 0;
@@ -247,7 +293,7 @@ cudaError_t launch_one(BoxState* b, const SegList& W, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if(e != cudaSuccess) return e;
     int per_sm = 0;
-    e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSeg, smem);
+    e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSeg + 32, smem);
     if(e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -256,29 +302,32 @@ cudaError_t launch_one(BoxState* b, const SegList& W, cudaStream_t s) {
   }
   const int64_t grid = std::min<int64_t>(W.nseg, resident);
   if(grid <= 0) return cudaSuccess;
-  kern<<<static_cast<unsigned>(grid), kSeg, smem, s>>>(b->p, W);
+  kern<<<static_cast<unsigned>(grid), kSeg + 32, smem, s>>>(b->p, W);
   return cudaGetLastError();
 }
 
 template <int LAT, int EQ, int ST>
 cudaError_t launch_tma(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots) {
   using L = Lattice<LAT>;
-  SegList W{};
-  W.segs_per_row = (b->p.nx + kSeg - 1) / kSeg;
-  W.err          = b->d_err;
+  SegList   W{};
+  const int spr = (b->p.nx + kSeg - 1) / kSeg;
+  int       nrows, nz;
   if(odd) {
-    W.y0      = L::D > 1 ? 1 : 0;
-    W.nrows_y = L::D > 1 ? b->p.ny - 2 : b->p.ny;
-    W.z0      = L::D > 2 ? 1 : 0;
-    const int nz = L::D > 2 ? b->p.nz - 2 : b->p.nz;
-    W.nseg    = (W.nrows_y > 0 && nz > 0) ? static_cast<int64_t>(W.segs_per_row) * W.nrows_y * nz : 0;
+    W.y0  = L::D > 1 ? 1 : 0;
+    nrows = L::D > 1 ? b->p.ny - 2 : b->p.ny;
+    W.z0  = L::D > 2 ? 1 : 0;
+    nz    = L::D > 2 ? b->p.nz - 2 : b->p.nz;
   } else {
-    W.y0      = 0;
-    W.nrows_y = b->p.ny;
-    W.z0      = 0;
-    W.nseg    = static_cast<int64_t>(W.segs_per_row) * b->p.ny * b->p.nz;
+    W.y0  = 0;
+    nrows = b->p.ny;
+    W.z0  = 0;
+    nz    = b->p.nz;
   }
-  *slots = W.nseg * (kSeg / 32);
+  W.nseg  = (nrows > 0 && nz > 0) ? spr * nrows * nz : 0;
+  W.spr   = make_fastdiv(static_cast<uint32_t>(spr));
+  W.nrows = make_fastdiv(static_cast<uint32_t>(std::max(nrows, 1)));
+  W.err   = b->d_err;
+  *slots = static_cast<int64_t>(W.nseg) * kConsumers;
   if(W.nseg == 0) return cudaSuccess;
   if(odd) {
     if(mom == 0) return launch_one<LAT, EQ, ST, true, 0>(b, W, s);

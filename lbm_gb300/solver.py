@@ -240,6 +240,22 @@ class BoxSolver:
         check(self._lib.lbm_gpu_box_autotune(self.ctx, C.byref(t)), self.ctx, "autotune")
         return t.value
 
+    def run_to(self, tol: float, check_interval: int = 1000, max_steps: int = 10 ** 7):
+        """Step until max(residual) < tol, checking every check_interval steps
+        (the reference's convergence loop with conv_interval = check_interval).
+        Returns (steps taken, last residual)."""
+        done = 0
+        res = np.full(self.nvar, np.inf)
+        while done < max_steps:
+            n = min(check_interval, max_steps - done)
+            self.step(n)
+            done += n
+            if n >= 2:
+                res = self.residual()
+                if float(np.max(res)) < tol:
+                    break
+        return done, res
+
     KERNELS = {"thread": 0, "staged": 1}
 
     def kernel(self, kind: Optional[str] = None) -> str:

@@ -247,7 +247,7 @@ static int find_dir(const blat_t* L, int cx, int cy, int cz) {
 /* the post-collision population arriving at (x,y,z) in direction k */
 static double pull(const ora_box* b, int x, int y, int z, int k, int allow_open) {
   const blat_t* L    = &b->L;
-  int           p[3] = {x, y, z}, s[3] = {0, 0, 0}, c[3] = {L->c[k][0], L->c[k][1], L->c[k][2]};
+  int           p[3] = {x, y, z}, s[3] = {x, y, z}, c[3] = {L->c[k][0], L->c[k][1], L->c[k][2]};
   int           bb = 0, open = 0;
   double        corr = 0;
   for(int a = 0; a < L->D; ++a) {

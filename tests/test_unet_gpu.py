@@ -1,0 +1,92 @@
+"""The warm-start U-Net's GPU kernels (BF16 tensor-core convolutions, their
+data and weight gradients, pooling, upsampling, loss) against the NumPy
+oracle of the same network with the same BF16 roundings."""
+import numpy as np
+import pytest
+
+from unet_ref import RefUNet, r16
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def pair():
+    from lbm_gb300.warmstart import UNet, layer_specs
+
+    B, H, W = 2, 16, 32
+    net = UNet(B, H, W, seed=3)
+    rng = np.random.default_rng(5)
+    x = (rng.normal(size=(B, H, W, 32)) * 0.5).astype(np.float32)
+    target = rng.normal(size=(B, H, W, 3)).astype(np.float32)
+    fluid = rng.random((B, H, W)) > 0.2
+    net.set_batch(x, target, fluid)
+    loss = net.loss_and_grad()
+    ref = RefUNet(layer_specs(), net.get_params())
+    rloss, rgrads = ref.loss_grad(x, target, fluid)
+    # the same network without any BF16 rounding: how far rounding alone moves each gradient
+    _, exact = RefUNet(layer_specs(), net.get_params(), bf16=False).loss_grad(x, target, fluid)
+    return net, ref, loss, rloss, rgrads, exact
+
+
+def test_forward_matches_oracle(pair):
+    net, ref, *_ = pair
+    for name in ("e0a", "pool0", "b_b", "d2b", "d0b"):
+        got = net.a[name].float().cpu().numpy()
+        assert rel(got, ref.a[name]) < 1e-2, name
+    out = net.a["out"].cpu().numpy()
+    assert rel(out, ref.a["out"]) < 1e-2
+
+
+def test_loss_and_every_gradient_match_oracle(pair):
+    """Every layer's weight and bias gradient agrees with the BF16 oracle
+    within 3%, or, for the deepest layers of the backward pass where BF16
+    rounding flips compound, within 3/4 of the distance that BF16 rounding
+    itself puts between the oracle and its unrounded FP64 twin."""
+    net, ref, loss, rloss, rgrads, exact = pair
+    assert abs(loss - rloss) <= 1e-3 * rloss
+    g = net.g32.cpu().numpy()
+    for name, cin, cout, _ in net.specs:
+        o, ob, _ = net.off[name]
+        gw = g[o:ob].reshape(cout, 9 * cin)
+        gb = g[ob:ob + cout]
+        rw, rb = rgrads[name]
+        tol_w = max(3e-2, 0.75 * rel(rw, exact[name][0]))
+        tol_b = max(3e-2, 0.75 * rel(rb, exact[name][1]))
+        assert rel(gw, rw) < tol_w, (name, rel(gw, rw), tol_w)
+        assert rel(gb, rb) < tol_b, (name, rel(gb, rb), tol_b)
+        # and the direction is right: cosine with the exact gradient
+        cos = float(np.dot(gw.ravel(), exact[name][0].ravel()) / (np.linalg.norm(gw) * np.linalg.norm(exact[name][0])))
+        assert cos > 0.95, (name, cos)
+
+
+def test_adam_step_lowers_the_loss():
+    from lbm_gb300.warmstart import UNet
+
+    net = UNet(2, 16, 32, seed=1)
+    rng = np.random.default_rng(2)
+    x = (rng.normal(size=(2, 16, 32, 32)) * 0.5).astype(np.float32)
+    t = rng.normal(size=(2, 16, 32, 3)).astype(np.float32) * 0.3
+    net.set_batch(x, t, np.ones((2, 16, 32), dtype=bool))
+    first = net.loss_and_grad()
+    for _ in range(60):
+        net.adam(lr=2e-3)
+        last = net.loss_and_grad()
+    assert last < 0.5 * first
+
+
+def test_trained_network_warm_start_saves_steps():
+    """End to end at a small scale (128 x 32 channels, Re 30-60): FP32
+    training fields, training with the project's kernels, then the plain FP64
+    LBM from rest and from the prediction to the same residual: the warm start
+    needs fewer steps."""
+    from lbm_gb300 import warmstart as ws
+
+    out = ws.experiment(n_train=48, per_batch=16, train_steps=20000, epochs=30, n_eval=8, per_eval=4, tol=1e-7, max_steps=200000,
+                        nx=128, ny=32, batch=8, re_range=(30.0, 60.0), lr=2e-3, log=None)
+    print({k: v for k, v in out.items() if k != "eval"}, out["eval"])
+    assert all(r["cold_res"] < 1e-7 and r["warm_res"] < 1e-7 for r in out["eval"])
+    assert out["steps_ratio"] < 0.9
