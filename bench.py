@@ -252,6 +252,21 @@ def poiseuille_run(args):
             "analytic_max_rel_dev_after_20000": float(np.abs(ux - exact).max() / exact.max())}
 
 
+def warmstart_run(args):
+    """Learned warm start, D2Q9 forced channel 511x128 with 1-8 cylinders, Re
+    20-200: FP32 training fields, U-Net training with the project's BF16
+    tensor-core kernels, then held-out channels by the plain FP64 LBM from
+    rest and from the prediction to residual 1e-8 (per channel)."""
+    from lbm_gb300 import warmstart as ws
+
+    out = ws.experiment(n_train=args.ws_train, per_batch=64, train_steps=args.ws_train_steps, epochs=args.ws_epochs, n_eval=16,
+                        per_eval=8, tol=1e-8, max_steps=args.max_steps, log=lambda m: print(m, file=sys.stderr, flush=True))
+    return {"metric": "learned warm start: wall time to residual 1e-8, warm / from rest", "value": out["wall_ratio"],
+            "unit": "ratio", "higher_is_better": False, "dtype": "f64 (LBM), bf16 (network)",
+            "config": {"workload": "D2Q9 forced channel 511x128, 1-8 cylinders r 6-20, Re 20-200, U-Net 4 levels width 32",
+                       "n_train": out["n_train"], "train_steps": out["train_steps"], "epochs": out["epochs"]}, "detail": out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -260,9 +275,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
-    ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann solves")
+    ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
+    ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
+    ap.add_argument("--ws-train-steps", type=int, default=200000, help="warm start: FP32 steps per training field")
+    ap.add_argument("--ws-epochs", type=int, default=20, help="warm start: training epochs")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
@@ -282,7 +300,7 @@ def main():
         args.warmup = 3
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
-            fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run}[args.workload]
+            fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run}[args.workload]
             print(json.dumps(fn(args)))
         return
 

@@ -16,7 +16,11 @@ residual as from rest.
   channels; several channels with one Reynolds number run together as the
   z-slices of one D2Q9 box.
 * Warm start: f = f_eq(rho, u) + f_neq, f_neq from the Chapman-Enskog
-  estimate -3 tau w_i rho Q_i:grad(u) of the predicted velocity gradient.
+  estimate -3 tau w_i rho Q_i:grad(u) of the predicted velocity gradient,
+  then two period-2 filters (at the first step and after 2,000 steps) that
+  remove the undamped staggered mode a non-rest initial state excites.  The
+  timing of the warm start includes the prediction, the population build and
+  the filters.
 """
 from __future__ import annotations
 
@@ -316,13 +320,27 @@ class UNet:
 
 # ---- inputs, targets, warm start ------------------------------------------------
 
+def net_width(nx: int) -> int:
+    """Network width for an nx-wide periodic channel: nx rounded up to a
+    multiple of 8 (the extra columns wrap around periodically)."""
+    return (nx + 7) // 8 * 8
+
+
+def wrap_columns(a: np.ndarray, W: int) -> np.ndarray:
+    """Extend the x axis (axis 1) of a periodic field to W columns."""
+    nx = a.shape[1]
+    return a[:, np.arange(W) % nx] if W != nx else a
+
+
 def input_channels(flags2d: np.ndarray, re: float) -> np.ndarray:
-    """(H, W, 32) network input of one channel geometry (flags (ny, nx))."""
-    H, W = flags2d.shape
+    """(H, W, 32) network input of one channel geometry (flags (ny, nx)),
+    W = net_width(nx): fluid mask, Re / 200, x / nx, y / ny, zeros."""
+    H, nx = flags2d.shape
+    W = net_width(nx)
     x = np.zeros((H, W, 32), dtype=np.float32)
-    x[..., 0] = (flags2d != cases.SOLID).astype(np.float32)
+    x[..., 0] = wrap_columns((flags2d != cases.SOLID).astype(np.float32), W)
     x[..., 1] = re / 200.0
-    x[..., 2] = (np.arange(W)[None, :] + 0.5) / W
+    x[..., 2] = ((np.arange(W) % nx)[None, :] + 0.5) / nx
     x[..., 3] = (np.arange(H)[:, None] + 0.5) / H
     return x
 
@@ -366,26 +384,49 @@ def populations_from_fields(rho: np.ndarray, ux: np.ndarray, uy: np.ndarray, sol
     return f.reshape(9, -1)
 
 
+def period2_filter(g) -> None:
+    """Replace the state s(t) by (s(t) + s(t+1)) / 2 (one step taken).
+
+    A warm-start state, unlike the state at rest, has a component along the
+    undamped period-2 (staggered) mode of BGK + bounce-back: left alone it
+    keeps the one-step residual near 1e-4 for ever.  Averaging two consecutive
+    states removes the eigenvalue -1 component exactly (to first order) and
+    halves every other mode's amplitude by (1 + lambda) / 2."""
+    s0 = g.populations()
+    g.step(1)
+    s1 = g.populations()
+    g.set_populations(0.5 * (s0 + s1))
+
+
 def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[float] = None, check: int = 2000,
-              init: Optional[np.ndarray] = None) -> Dict:
+              init: Optional[np.ndarray] = None, filters=(0, 2000)) -> Dict:
     """Forced channels sharing one Re as the z-slices of one D2Q9 box, from
     rest (or from populations `init`, (9, ncells)), for max_steps or until the
     residual summed over the slices, divided by their number, is below tol
     (checked every `check` steps: the reference's convergence test with
-    conv_interval = check).  Returns fields, steps, wall time, residual."""
+    conv_interval = check).  A warm start applies period2_filter at the steps
+    in `filters`.  Returns fields, steps, wall time, residual."""
     from .solver import BoxSolver
 
     st = cases.stacked_forced(chans)
     g = BoxSolver(st["lattice"], st["shape"], st["omega"], storage, **cases.box_kwargs(st))
     g.initial_condition()
+    g.synchronize()
+    t0 = time.perf_counter()
+    pending = sorted(filters) if init is not None else []
     if init is not None:
         g.set_populations(init)
     n = len(chans)
-    g.synchronize()
-    t0 = time.perf_counter()
     done, res = 0, np.full(3, np.inf)
     while done < max_steps:
+        if pending and pending[0] <= done:
+            pending.pop(0)
+            period2_filter(g)
+            done += 1
+            continue
         k = min(check, max_steps - done)
+        if pending:
+            k = min(k, max(2, pending[0] - done))
         g.step(k)
         done += k
         if tol is not None:
@@ -414,10 +455,11 @@ def make_dataset(seeds: List[int], per_batch: int, steps: int, storage: str = "f
         re = float(rng.uniform(*re_range))
         chans = [cases.forced_channel(s, nx, ny, re=re) for s in seeds[k:k + per_batch]]
         out = run_stack(chans, storage, steps)
+        W = net_width(nx)
         for j, c in enumerate(chans):
             xs.append(input_channels(c["flags"], re))
-            ys.append(np.stack([out["rho"][j], out["ux"][j], out["uy"][j]], axis=-1))
-            masks.append(c["flags"] != cases.SOLID)
+            ys.append(wrap_columns(np.stack([out["rho"][j], out["ux"][j], out["uy"][j]], axis=-1), W))
+            masks.append(wrap_columns(c["flags"] != cases.SOLID, W))
         res.append(out["residual"])
         if log:
             log(f"dataset batch {k // per_batch}: Re {re:.1f}, {len(chans)} channels, {steps} steps, residual/slice {out['residual']:.2e}, "
@@ -457,8 +499,9 @@ def predict_fields(net: "UNet", chans: List[Dict], scales: Scales) -> List[Tuple
         for j, c in enumerate(group):
             x[j] = input_channels(c["flags"], c["re"])
         y = net.predict(x)
-        for j in range(len(group)):
-            out.append(scales.from_net(y[j]))
+        for j, c in enumerate(group):
+            nx = c["flags"].shape[1]
+            out.append(scales.from_net(y[j][:, :nx]))
     return out
 
 
@@ -468,11 +511,16 @@ def warm_start_populations(chans: List[Dict], fields) -> np.ndarray:
 
 
 def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 300000, epochs: int = 20, n_eval: int = 16,
-               per_eval: int = 8, tol: float = 1e-8, max_steps: int = 1500000, nx: int = 512, ny: int = 128, batch: int = 8,
-               re_range=(20.0, 200.0), lr: float = 1e-3, log=print) -> Dict:
+               per_eval: int = 8, tol: float = 1e-8, max_steps: int = 1500000, nx: int = 511, ny: int = 128, batch: int = 8,
+               re_range=(20.0, 200.0), lr: float = 1e-3, filtered_rest: bool = True, log=print) -> Dict:
     """The whole warm-start study: FP32 training fields, training with the
     project's kernels, then for held-out channels the plain FP64 LBM from rest
-    and from the network's prediction to the same residual."""
+    and from the network's prediction to the same residual.
+
+    The periodic length is odd (511 by default): with an even one, some
+    geometries keep an undamped period-2 (staggered) mode of the BGK +
+    bounce-back scheme, seen identically in the CPU oracle, and the
+    reference's one-step residual then never falls below ~1e-4."""
     import torch
 
     t0 = time.perf_counter()
@@ -480,7 +528,7 @@ def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 3000
     t_data = time.perf_counter() - t0
     s_rho = float(np.std(data["fields"][..., 0][data["fluid"]])) or 1e-3
     scales = Scales(s_rho, 0.08)
-    net = UNet(batch, ny, nx, seed=0)
+    net = UNet(batch, ny, net_width(nx), seed=0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     losses = train(net, data, scales, epochs, lr=lr, log=log)
@@ -493,6 +541,11 @@ def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 3000
         re = float(rng.uniform(*re_range))
         chans = [cases.forced_channel(100000 + k + j, nx, ny, re=re) for j in range(per_eval)]
         cold = run_stack(chans, "f64", max_steps, tol)
+        # the same filters applied from rest, to separate their share of the gain from the network's
+        rest = None
+        if k == 0 and filtered_rest:
+            rest = run_stack(chans, "f64", max_steps, tol, init=warm_start_populations(
+                chans, [(np.ones((ny, nx)), np.zeros((ny, nx)), np.zeros((ny, nx))) for _ in chans]))
         tp = time.perf_counter()
         fields = predict_fields(net, chans, scales)
         init = warm_start_populations(chans, fields)
@@ -502,7 +555,8 @@ def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 3000
         u_pred = np.stack([f[1] for f in fields])
         err = float(np.linalg.norm((u_pred - cold["ux"])[fluid]) / np.linalg.norm(cold["ux"][fluid]))
         rows.append(dict(re=re, cold_steps=cold["steps"], cold_wall=cold["wall"], cold_res=cold["residual"], warm_steps=warm["steps"],
-                         warm_wall=warm["wall"] + t_pred, warm_res=warm["residual"], predict_s=t_pred, ux_rel_l2_pred=err))
+                         warm_wall=warm["wall"] + t_pred, warm_res=warm["residual"], predict_s=t_pred, ux_rel_l2_pred=err,
+                         rest_filtered_steps=rest["steps"] if rest else None))
         if log:
             log(f"held-out Re {re:.1f}: cold {cold['steps']} steps {cold['wall']:.1f} s, warm {warm['steps']} steps "
                 f"{warm['wall'] + t_pred:.1f} s, prediction u_x error {err:.3e}")

@@ -79,14 +79,14 @@ def test_adam_step_lowers_the_loss():
 
 
 def test_trained_network_warm_start_saves_steps():
-    """End to end at a small scale (128 x 32 channels, Re 30-60): FP32
+    """End to end at a small scale (127 x 32 channels, Re 30-60): FP32
     training fields, training with the project's kernels, then the plain FP64
     LBM from rest and from the prediction to the same residual: the warm start
     needs fewer steps."""
     from lbm_gb300 import warmstart as ws
 
-    out = ws.experiment(n_train=48, per_batch=16, train_steps=20000, epochs=30, n_eval=8, per_eval=4, tol=1e-7, max_steps=200000,
-                        nx=128, ny=32, batch=8, re_range=(30.0, 60.0), lr=2e-3, log=None)
+    out = ws.experiment(n_train=64, per_batch=16, train_steps=30000, epochs=60, n_eval=8, per_eval=4, tol=1e-7, max_steps=200000,
+                        nx=127, ny=32, batch=8, re_range=(30.0, 60.0), lr=2e-3, log=None)
     print({k: v for k, v in out.items() if k != "eval"}, out["eval"])
     assert all(r["cold_res"] < 1e-7 and r["warm_res"] < 1e-7 for r in out["eval"])
     assert out["steps_ratio"] < 0.9
