@@ -54,7 +54,7 @@ namespace {
 //   either order.
 // MOM: 0 plain, 1 also write the moments, 2 also accumulate |moments - previous|
 template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
+__global__ void __launch_bounds__(256, (MOM == 0 && ST != LBM_STORE_F64) ? 4 : 1) k_box_bulk(BoxParams P) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
