@@ -86,14 +86,21 @@ int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, d
 
 /* Threads per block the autotuner chose for the per-thread step kernel. */
 int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
-/* Bulk step kernel of a box context: LBM_BOX_KERNEL_THREAD (one global load
- * per population and thread) or LBM_BOX_KERNEL_STAGED (each CTA stages whole
- * rows in shared memory with bulk copies); lbm_gpu_create_box picks the faster
- * by timing both.  Both give bit-identical results.  kernel < 0 only queries.
- * LBM_ERR_UNSUPPORTED when the box does not qualify for staging (nx times the
- * storage size must be a multiple of 16 bytes). */
-typedef enum lbm_box_kernel { LBM_BOX_KERNEL_THREAD = 0, LBM_BOX_KERNEL_STAGED = 1 } lbm_box_kernel;
+/* Bulk step kernel of a box context: LBM_BOX_KERNEL_THREAD (one cell per
+ * thread, one global load per population), LBM_BOX_KERNEL_STAGED (each CTA
+ * stages whole rows in shared memory with bulk copies) or
+ * LBM_BOX_KERNEL_PAIRED (two x-adjacent cells per thread, 2-element loads and
+ * stores where aligned); lbm_gpu_create_box picks the fastest by timing them.
+ * All give bit-identical results.  kernel < 0 only queries.
+ * LBM_ERR_UNSUPPORTED when the box does not qualify: staging needs nx times
+ * the storage size to be a multiple of 16 bytes; pairing needs nx even and a
+ * 32- or 16-bit storage. */
+typedef enum lbm_box_kernel { LBM_BOX_KERNEL_THREAD = 0, LBM_BOX_KERNEL_STAGED = 1, LBM_BOX_KERNEL_PAIRED = 2 } lbm_box_kernel;
 int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected);
+/* The autotuner times even (local) and odd (streaming) steps separately and
+ * may pick a different kernel for each: the kernels of both parities
+ * (lbm_gpu_box_select_kernel sets both, and reports -1 when they differ). */
+int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd);
 
 /* Run nsteps exactly as lbm_gpu_step does, but with a CUDA event pair around
  * every launch of the step kernel on the context's stream: total_ms is the

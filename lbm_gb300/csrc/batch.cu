@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
       }
       C mom[NV9];
       C F[3] = {0, 0, 0};
-      collide_ns<LBM_D2Q9, C>(prm<C>(D.omega, D.omega_f), false, F, v, MOM ? mom : nullptr);
+      collide_ns<LBM_D2Q9, C, false>(prm<C>(D.omega, D.omega_f), false, F, v, MOM ? mom : nullptr);
       if constexpr(MOM != 0) {
         C* M = static_cast<C*>(P.mom) + D.mom_off;
 #pragma unroll

@@ -53,83 +53,192 @@ namespace {
 //   written by the one thread that owns it, so the two kernels may run in
 //   either order.
 // MOM: 0 plain, 1 also write the moments, 2 also accumulate |moments - previous|
+// One cell of the bulk step (the body of k_box_bulk; also the fallback of
+// k_box_pair for pairs that mix cell kinds).  Adds |moment change| to diff.
 template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__global__ void __launch_bounds__(256, (MOM == 0 && ST != LBM_STORE_F64) ? 4 : 1) k_box_bulk(BoxParams P) {
+__device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int z, int cell, uint8_t flag,
+                                          typename Store<ST>::C* diff) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  constexpr int NV   = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
-
-  const int  x     = blockIdx.x * blockDim.x + threadIdx.x;
-  const int  y     = blockIdx.y;
-  const int  z     = blockIdx.z;
-  const bool valid = x < P.nx;
-  const int  cell  = valid ? x + P.nx * (y + P.ny * z) : 0;
-  const uint8_t flag = valid ? P.flags[cell] : LBM_CELL_SOLID;
+  constexpr int NV = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
   const uint8_t type = flag & TYPE_MASK;
   T*            A    = static_cast<T*>(P.pop);
+  T* const      Ac   = A + cell;  // the cell's slot in plane 0
   const int     NA   = static_cast<int>(P.nalloc);
-  C             diff[NV];
-#pragma unroll
-  for(int k = 0; k < NV; ++k) diff[k] = C(0);
-
-  bool work;
-  if constexpr(ODD) work = type == LBM_CELL_FLUID && !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+  bool          work;
+  if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
   else work = type != LBM_CELL_SOLID;
-
-  if(work) {
-    C f[Q];
-    C mom[NV], prev[NV];
+  if(!work) return;
+  C f[Q];
+  C mom[NV], prev[NV];
 #pragma unroll
-    for(int k = 0; k < NV; ++k) mom[k] = 0;
-    prefetch_moments<C, MOM, NV>(P, cell, prev);
-    const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
-    if(emit) {
-      emit_equilibrium<LAT, EQ, C>(P, f, cell);
-    } else {
-      if constexpr(!ODD) {
-        static_for<Q>([&](auto qc) {
-          constexpr int q = decltype(qc)::value;
-          f[q]            = S::load(A[q * NA + cell]);
-        });
-        if(type == LBM_CELL_OUTLET) {
-          // links from beyond +x: what the upstream cell received (ghost plane)
-          static_for<Q>([&](auto qc) {
-            constexpr int q = decltype(qc)::value;
-            if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
-          });
-        }
-      } else {
-        const int sy = P.nx, sz = P.nx * P.ny;
-        static_for<Q>([&](auto qc) {
-          constexpr int q   = decltype(qc)::value;
-          const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-          f[q]              = S::load(A[L::opp(q) * NA + cell - off]);
-        });
-      }
-      collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
-    }
-    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
+  for(int k = 0; k < NV; ++k) mom[k] = 0;
+  prefetch_moments<C, MOM, NV>(P, cell, prev);
+  const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+  if(emit) {
+    emit_equilibrium<LAT, EQ, C>(P, f, cell);
+  } else {
     if constexpr(!ODD) {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        A[L::opp(q) * NA + cell] = S::store(f[q]);
+        f[q]            = S::load(Ac[q * NA]);
       });
+      if(type == LBM_CELL_OUTLET) {
+        // links from beyond +x: what the upstream cell received (ghost plane)
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+        });
+      }
     } else {
       const int sy = P.nx, sz = P.nx * P.ny;
       static_for<Q>([&](auto qc) {
         constexpr int q   = decltype(qc)::value;
         const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-        A[q * NA + cell + off] = S::store(f[q]);
+        f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
       });
     }
+    collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
+  }
+  moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
+  if constexpr(!ODD) {
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      Ac[L::opp(q) * NA] = S::store(f[q]);
+    });
+  } else {
+    const int sy = P.nx, sz = P.nx * P.ny;
+    static_for<Q>([&](auto qc) {
+      constexpr int q   = decltype(qc)::value;
+      const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+      Ac[q * NA + off]  = S::store(f[q]);
+    });
+  }
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+__global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
+  using C          = typename Store<ST>::C;
+  constexpr int NV = EQ == LBM_NAVIER_STOKES ? Lattice<LAT>::D + 1 : 1;
+  const int     x  = blockIdx.x * blockDim.x + threadIdx.x;
+  const int     y  = blockIdx.y;
+  const int     z  = blockIdx.z;
+  C             diff[NV];
+#pragma unroll
+  for(int k = 0; k < NV; ++k) diff[k] = C(0);
+  if(x < P.nx) {
+    const int cell = x + P.nx * (y + P.ny * z);
+    bulk_cell<LAT, EQ, ST, ODD, MOM>(P, x, y, z, cell, P.flags[cell], diff);
   }
   if constexpr(MOM == 2) {
     const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
     warp_partials<NV>(diff, P.partials, P.partial_stride, b * (blockDim.x >> 5) + (threadIdx.x >> 5));
   }
+}
+
+// Two populations of adjacent cells as one aligned load / store.
+template <int ST>
+struct Pair;
+template <>
+struct Pair<LBM_STORE_F32> {
+  static __device__ __forceinline__ void load(const float* p, float& a, float& b) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    a              = v.x;
+    b              = v.y;
+  }
+  static __device__ __forceinline__ void store(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+};
+template <>
+struct Pair<LBM_STORE_F16_DEV> {
+  static __device__ __forceinline__ void load(const __half* p, float& a, float& b) {
+    const float2 v = __half22float2(*reinterpret_cast<const __half2*>(p));
+    a              = v.x;
+    b              = v.y;
+  }
+  static __device__ __forceinline__ void store(__half* p, float a, float b) { *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b); }
+};
+template <>
+struct Pair<LBM_STORE_BF16_DEV> {
+  static __device__ __forceinline__ void load(const __nv_bfloat16* p, float& a, float& b) {
+    const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+    a              = v.x;
+    b              = v.y;
+  }
+  static __device__ __forceinline__ void store(__nv_bfloat16* p, float a, float b) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+  }
+};
+
+// k_box_pair: the plain (MOM = 0) bulk step with two x-adjacent cells per
+// thread (nx even, so a pair never straddles a row and starts on an even
+// cell).  Directions with c_x = 0 move both populations with one 2-element
+// load and store; the others, one element apart from alignment, use two.
+// Two independent collisions per thread also double the arithmetic in flight.
+// Pairs that are not two plain fluid cells (even step) or two interior bulk
+// cells (odd step) fall back to bulk_cell, cell by cell.
+template <int LAT, int EQ, int ST, bool ODD>
+__global__ void __launch_bounds__(256) k_box_pair(BoxParams P) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  using PR        = Pair<ST>;
+  constexpr int Q = L::Q;
+  const int     x = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int     y = blockIdx.y;
+  const int     z = blockIdx.z;
+  if(x >= P.nx) return;
+  const int      cell = x + P.nx * (y + P.ny * z);
+  const uint16_t fl2  = *reinterpret_cast<const uint16_t*>(P.flags + cell);
+  const uint8_t  fa = static_cast<uint8_t>(fl2 & 0xff), fb = static_cast<uint8_t>(fl2 >> 8);
+  bool           fast;
+  if constexpr(ODD) fast = fa == LBM_CELL_FLUID && fb == LBM_CELL_FLUID;  // both fluid, neither LINKED
+  else fast = (fa & TYPE_MASK) == LBM_CELL_FLUID && (fb & TYPE_MASK) == LBM_CELL_FLUID;
+  if(!fast) {
+    C d[1];
+    bulk_cell<LAT, EQ, ST, ODD, 0>(P, x, y, z, cell, fa, d);
+    bulk_cell<LAT, EQ, ST, ODD, 0>(P, x + 1, y, z, cell + 1, fb, d);
+    return;
+  }
+  T* const  Ac = static_cast<T*>(P.pop) + cell;  // the pair's first slot in plane 0
+  const int NA = static_cast<int>(P.nalloc);
+  const int sy = P.nx, sz = P.nx * P.ny;
+  C         f0[Q], f1[Q];
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if constexpr(!ODD) {
+      PR::load(Ac + q * NA, f0[q], f1[q]);
+    } else {
+      const int off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+      const T*  src = Ac + (L::opp(q) * NA - off);
+      if constexpr(L::c(q, 0) == 0) {
+        PR::load(src, f0[q], f1[q]);
+      } else {
+        f0[q] = S::load(src[0]);
+        f1[q] = S::load(src[1]);
+      }
+    }
+  });
+  collide<LAT, EQ, C>(P, f0, nullptr);
+  collide<LAT, EQ, C>(P, f1, nullptr);
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if constexpr(!ODD) {
+      PR::store(Ac + L::opp(q) * NA, f0[q], f1[q]);
+    } else {
+      const int off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+      T*        dst = Ac + (q * NA + off);
+      if constexpr(L::c(q, 0) == 0) {
+        PR::store(dst, f0[q], f1[q]);
+      } else {
+        dst[0] = S::store(f0[q]);
+        dst[1] = S::store(f1[q]);
+      }
+    }
+  });
 }
 
 // Link tables of the boundary cells, built once: for list entry i and
@@ -190,6 +299,11 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
 #pragma unroll
     for(int k = 0; k < NV; ++k) mom[k] = 0;
     prefetch_moments<C, MOM, NV>(P, cell, prev);
+    // every table entry is read before the first population store: a table
+    // load issued after a store would wait behind it (the compiler cannot
+    // prove the two do not alias), one memory round trip per direction
+    int32_t dsts[Q];
+    static_for<Q>([&](auto qc) { dsts[decltype(qc)::value] = dst[decltype(qc)::value * n + i]; });
     if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
       emit_equilibrium<LAT, EQ, C>(P, f, cell);
     } else {
@@ -200,11 +314,12 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
       });
       collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
     }
+    if(corr_dst)
+      static_for<Q>([&](auto qc) { f[decltype(qc)::value] += static_cast<C>(corr_dst[decltype(qc)::value * n + i]); });
     moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      const int32_t d = dst[q * n + i];
-      if(d >= 0) A[d] = S::store(corr_dst ? f[q] + static_cast<C>(corr_dst[q * n + i]) : f[q]);
+      if(dsts[q] >= 0) A[dsts[q]] = S::store(f[q]);
     });
   }
   if constexpr(MOM == 2) warp_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
@@ -451,12 +566,18 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   if(ev0) cudaEventRecord(ev0, s);
   int64_t        nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel
   const unsigned nbb   = static_cast<unsigned>((b->n_bnd + 127) / 128);
-  if(b->use_tma) {
+  const int      kind   = odd ? b->kind_odd : b->kind_even;
+  const bool     staged = kind == LBM_BOX_KERNEL_STAGED;
+  const bool     paired = kind == LBM_BOX_KERNEL_PAIRED && mom == 0;  // residual steps use the per-thread kernel
+  const dim3     gp(static_cast<unsigned>((b->p.nx / 2 + tpb - 1) / tpb), static_cast<unsigned>(b->p.ny), static_cast<unsigned>(b->p.nz));
+  if(staged) {
     const cudaError_t e = box_tma_bulk(b, odd, mom, s, &nbulk);
     if(e != cudaSuccess) return e;
   }
   if(odd) {
-    if(b->use_tma) {
+    if(staged) {
+    } else if(paired) {
+      if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, true><<<gp, tpb, 0, s>>>(b->p);
     } else if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
@@ -467,7 +588,9 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     }
     if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
-    if(b->use_tma) {
+    if(staged) {
+    } else if(paired) {
+      if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, false><<<gp, tpb, 0, s>>>(b->p);
     } else if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
@@ -535,7 +658,7 @@ int cerr(std::string& err, cudaError_t e, const char* what) {
 
 // a staged kernel that gave up waiting for its copies leaves a flag behind
 int check_wait_flag(BoxState* b, std::string& err) {
-  if(!b->use_tma) return LBM_OK;
+  if(b->kind_even != LBM_BOX_KERNEL_STAGED && b->kind_odd != LBM_BOX_KERNEL_STAGED) return LBM_OK;
   int         flag = 0;
   cudaError_t e    = cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if(e != cudaSuccess) return cerr(err, e, "wait flag");
@@ -545,6 +668,13 @@ int check_wait_flag(BoxState* b, std::string& err) {
     return LBM_ERR_CUDA;
   }
   return LBM_OK;
+}
+
+bool box_kernel_supported(const BoxState* b, int kind) {
+  if(kind == LBM_BOX_KERNEL_THREAD) return true;
+  if(kind == LBM_BOX_KERNEL_STAGED) return box_tma_supported(b);
+  if(kind == LBM_BOX_KERNEL_PAIRED) return b->p.nx % 2 == 0 && b->desc.storage != LBM_STORE_F64;
+  return false;
 }
 
 void drop_graphs(BoxState* b) {
@@ -745,6 +875,34 @@ float time_pair(BoxState* b, int tpb, cudaStream_t s) {
   return ms;
 }
 
+// time the even and the odd step separately: the fastest of four of each,
+// after two warm-up pairs
+void time_parities(BoxState* b, cudaStream_t s, float* even_ms, float* odd_ms) {
+  cudaEvent_t ev[3];
+  for(auto& e : ev) cudaEventCreate(&e);
+  for(int k = 0; k < 2; ++k) {
+    dispatch_step(b, false, 0, s);
+    dispatch_step(b, true, 0, s);
+  }
+  float te = 1e30f, to = 1e30f;
+  for(int k = 0; k < 4; ++k) {
+    cudaEventRecord(ev[0], s);
+    dispatch_step(b, false, 0, s);
+    cudaEventRecord(ev[1], s);
+    dispatch_step(b, true, 0, s);
+    cudaEventRecord(ev[2], s);
+    cudaEventSynchronize(ev[2]);
+    float a = 0, c = 0;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&c, ev[1], ev[2]);
+    te = std::min(te, a);
+    to = std::min(to, c);
+  }
+  for(auto& e : ev) cudaEventDestroy(e);
+  *even_ms = te;
+  *odd_ms  = to;
+}
+
 }  // namespace lbm
 
 using namespace lbm;
@@ -870,7 +1028,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
           }
       const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && (D < 3 || (z > 0 && z < nz - 1));
       if(near || !inside || hflags[i] != LBM_CELL_FLUID) list.push_back(static_cast<int32_t>(i));
-      if(near) hflags[i] = static_cast<uint8_t>(hflags[i] | NEAR_SOLID);
+      if(near || !inside) hflags[i] = static_cast<uint8_t>(hflags[i] | LINKED);
     }
     b->n_bnd = static_cast<int64_t>(list.size());
     if(e == cudaSuccess) e = cudaMalloc(&b->bnd_list, sizeof(int32_t) * std::max<size_t>(1, list.size()));
@@ -941,15 +1099,30 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
         b->tuned_tpb = tpb;
       }
     }
-    // the bulk-copy staged bulk kernel, where the box allows it
-    if(box_tma_supported(b)) {
-      b->use_tma     = 1;
-      const float ms = time_pair(b, b->tuned_tpb, stream);
+    // then every bulk kernel the box allows, timed per step parity: the even
+    // (local) and odd (streaming) steps may each take a different one
+    float best_even = 1e30f, best_odd = 1e30f;
+    int   pick_even = LBM_BOX_KERNEL_THREAD, pick_odd = LBM_BOX_KERNEL_THREAD;
+    for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED}) {
+      if(!box_kernel_supported(b, kind)) continue;
+      b->kind_even = b->kind_odd = kind;
+      float       ev = 0, od = 0;
+      time_parities(b, stream, &ev, &od);
       int         flag = 0;
       cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
-      b->use_tma = (ms < best && flag == 0) ? 1 : 0;
       cudaMemset(b->d_err, 0, sizeof(int));
+      if(flag) continue;
+      if(ev < best_even) {
+        best_even = ev;
+        pick_even = kind;
+      }
+      if(od < best_odd) {
+        best_odd = od;
+        pick_odd = kind;
+      }
     }
+    b->kind_even = pick_even;
+    b->kind_odd  = pick_odd;
     cudaMemsetAsync(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1), stream);
     if(cudaStreamSynchronize(stream) != cudaSuccess) {
       cudaStreamDestroy(stream);
@@ -1056,17 +1229,26 @@ int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block) {
 
 int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected) {
   BoxState* b = lbm_internal_box(ctx);
-  if(!b || kernel > LBM_BOX_KERNEL_STAGED) return LBM_ERR_INVALID;
-  if(kernel == LBM_BOX_KERNEL_STAGED && !box_tma_supported(b)) {
-    lbm_internal_set_error(ctx, "box does not qualify for the staged kernel (rows must be 16-byte multiples)");
+  if(!b || kernel > LBM_BOX_KERNEL_PAIRED) return LBM_ERR_INVALID;
+  if(kernel >= 0 && !box_kernel_supported(b, kernel)) {
+    lbm_internal_set_error(ctx, kernel == LBM_BOX_KERNEL_STAGED ? "box does not qualify for the staged kernel (rows must be 16-byte multiples)"
+                                                               : "box does not qualify for the paired kernel (nx even, FP32/FP16/BF16 storage)");
     return LBM_ERR_UNSUPPORTED;
   }
-  if(kernel >= 0 && kernel != b->use_tma) {
+  if(kernel >= 0 && (kernel != b->kind_even || kernel != b->kind_odd)) {
     cudaStreamSynchronize(lbm_internal_stream(ctx));
     drop_graphs(b);
-    b->use_tma = kernel;
+    b->kind_even = b->kind_odd = kernel;
   }
-  if(selected) *selected = b->use_tma;
+  if(selected) *selected = b->kind_even == b->kind_odd ? b->kind_even : -1;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b) return LBM_ERR_INVALID;
+  if(even) *even = b->kind_even;
+  if(odd) *odd = b->kind_odd;
   return LBM_OK;
 }
 

@@ -72,7 +72,8 @@ struct BoxState {
   double*      corr_src  = nullptr;  // moving-wall terms (allocated only when a wall moves)
   double*      corr_dst  = nullptr;
   int64_t      res_slots = 0;        // partial slots written by the last residual step
-  int          use_tma   = 0;        // bulk kernel: 0 per-thread loads, 1 bulk-copy staged (box_tma.cu)
+  int          kind_even = 0;        // lbm_box_kernel of the even steps: per-thread, staged (box_tma.cu) or paired
+  int          kind_odd  = 0;        // and of the odd steps
   int*         d_err     = nullptr;  // set by a staged kernel whose bounded wait ran out
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
 };

@@ -15,7 +15,8 @@
 namespace lbm {
 
 constexpr uint8_t TYPE_MASK  = 0x07;
-constexpr uint8_t NEAR_SOLID = 0x08;  // set by the engine: a neighbour is solid
+constexpr uint8_t LINKED     = 0x08;  // set by the engine: the odd step resolves this cell's links in the
+                                     // boundary kernel (a solid neighbour, or a face of the box)
 // ---- link resolution ---------------------------------------------------------
 // mirror of direction q in the axes of `mask` (free-slip reflection)
 template <int LAT>
@@ -113,7 +114,8 @@ __device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
     F[0] = prm<C>(P.force[0], P.force_f[0]);
     F[1] = prm<C>(P.force[1], P.force_f[1]);
     F[2] = prm<C>(P.force[2], P.force_f[2]);
-    collide_ns<LAT, C>(prm<C>(P.omega, P.omega_f), P.has_force != 0, F, v, mom_out);
+    if(P.has_force) collide_ns<LAT, C, true>(prm<C>(P.omega, P.omega_f), true, F, v, mom_out);
+    else collide_ns<LAT, C, false>(prm<C>(P.omega, P.omega_f), false, F, v, mom_out);
   } else {
     collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
                             mom_out);

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
     const uint8_t flag  = valid ? P.flags[cell] : LBM_CELL_SOLID;
     const uint8_t type  = flag & TYPE_MASK;
     bool          work;
-    if constexpr(ODD) work = type == LBM_CELL_FLUID && !(flag & NEAR_SOLID) && interior<LAT>(P, x, y, z);
+    if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
     else work = type != LBM_CELL_SOLID;
     const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     C          mom[NV], prev[NV], diff[NV];

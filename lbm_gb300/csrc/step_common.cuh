@@ -91,8 +91,16 @@ __device__ __forceinline__ C prm(double d, float f) {
 //   v' = (1 - omega) v + omega v_eq + S (1 - omega/2) [3 (c - u).F + 9 (c.u)(c.F)].
 // Opposite directions share the even part of v_eq and of the forcing term and
 // differ in the sign of the odd part, so each pair costs one evaluation.
-template <int LAT, class C>
-__device__ __forceinline__ void collide_ns(C om, bool force, const C* Fin, C* v, C* mom_out) {
+// 1/x: the correctly rounded single-precision reciprocal (no division
+// slow path); plain division in FP64
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
+
+// FORCE is a compile-time switch: without a body force the forcing terms and
+// their branches are not generated at all.
+template <int LAT, class C, bool FORCE = true>
+__device__ __forceinline__ void collide_ns(C om, bool force_in, const C* Fin, C* v, C* mom_out) {
+  const bool force = FORCE && force_in;
   using L         = Lattice<LAT>;
   constexpr int Q = L::Q, D = L::D;
   constexpr C   S = static_cast<C>(STATE_SCALE), IS = static_cast<C>(1.0 / STATE_SCALE);
@@ -108,15 +116,19 @@ __device__ __forceinline__ void collide_ns(C om, bool force, const C* Fin, C* v,
     });
   });
   const C    rho   = C(1) + r0 * IS;
-  const C    irho  = C(1) / rho;
+  const C    irho  = recip(rho);
   C F[3] = {0, 0, 0}, u[3] = {0, 0, 0};
   if(force) static_for<D>([&](auto dc) { F[decltype(dc)::value] = Fin[decltype(dc)::value]; });
   C usq = 0, uf = 0;
   static_for<D>([&](auto dc) {
     constexpr int d = decltype(dc)::value;
-    u[d]            = fma(j[d], IS, C(0.5) * F[d]) * irho;
-    usq             = fma(u[d], u[d], usq);
-    uf              = fma(u[d], F[d], uf);
+    if constexpr(FORCE) {
+      u[d] = fma(j[d], IS, C(0.5) * F[d]) * irho;
+      uf   = fma(u[d], F[d], uf);
+    } else {
+      u[d] = j[d] * IS * irho;
+    }
+    usq = fma(u[d], u[d], usq);
   });
   if(mom_out) {
     mom_out[0] = rho;
@@ -135,14 +147,17 @@ __device__ __forceinline__ void collide_ns(C om, bool force, const C* Fin, C* v,
     constexpr int q = decltype(qc)::value;
     constexpr int o = L::opp(q);
     if constexpr(q < o) {
-      C cu = 0, cf = 0;
+      // c_q.u and c_q.F, started from the first non-zero component (no 0 + x)
+      constexpr int d0 = L::c(q, 0) != 0 ? 0 : (L::c(q, 1) != 0 ? 1 : 2);
+      C             cu = L::c(q, d0) > 0 ? u[d0] : -u[d0];
+      C             cf = L::c(q, d0) > 0 ? F[d0] : -F[d0];
       static_for<D>([&](auto dc) {
         constexpr int d = decltype(dc)::value;
-        if constexpr(L::c(q, d) > 0) {
+        if constexpr(d > d0 && L::c(q, d) > 0) {
           cu += u[d];
           cf += F[d];
         }
-        if constexpr(L::c(q, d) < 0) {
+        if constexpr(d > d0 && L::c(q, d) < 0) {
           cu -= u[d];
           cf -= F[d];
         }

@@ -256,15 +256,21 @@ class BoxSolver:
                     break
         return done, res
 
-    KERNELS = {"thread": 0, "staged": 1}
+    KERNELS = {"thread": 0, "staged": 1, "paired": 2}
 
     def kernel(self, kind: Optional[str] = None) -> str:
-        """The bulk step kernel in use ("thread" or "staged"); with `kind`,
-        switch to it first (both give bit-identical results)."""
+        """The bulk step kernel in use ("thread", "staged" or "paired", or
+        "even/odd" when the autotuner chose one per step parity); with `kind`,
+        switch both parities to it first (all give bit-identical results)."""
         sel = C.c_int32()
         check(self._lib.lbm_gpu_box_select_kernel(self.ctx, -1 if kind is None else self.KERNELS[kind], C.byref(sel)), self.ctx,
               "select_kernel")
-        return "staged" if sel.value == 1 else "thread"
+        names = {0: "thread", 1: "staged", 2: "paired"}
+        if sel.value >= 0:
+            return names[sel.value]
+        ev, od = C.c_int32(), C.c_int32()
+        check(self._lib.lbm_gpu_box_kernels(self.ctx, C.byref(ev), C.byref(od)), self.ctx, "kernels")
+        return f"{names[ev.value]}/{names[od.value]}"
 
 
 # ---- the reference's run loop -------------------------------------------------
