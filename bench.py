@@ -39,6 +39,10 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 D3Q19 = 4
 B_PER_CELL = {"f64": 2 * 19 * 8 + 1, "f32": 2 * 19 * 4 + 1, "f16dev": 2 * 19 * 2 + 1, "bf16dev": 2 * 19 * 2 + 1}
 METRIC = "MLUPS (D3Q19 sphere 512x256x256, FP16-deviation storage)"
+# DRAM bytes (read + write) per step of this workload, averaged over the two
+# step parities (bulk + boundary + outlet kernels), from the one-pass ncu
+# launch list recorded in profiles/launches_bench_d3q19_sphere_512x256x256.md
+MEASURED_TRAFFIC_PER_STEP = {"f16dev": 2.71e9}
 
 
 def peaks():
@@ -284,6 +288,7 @@ def main():
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
+    ap.add_argument("--kernel", default=None, choices=["thread", "staged", "paired"], help="--profile-case: force this bulk kernel")
     args = ap.parse_args()
     if args.profile_case:
         from lbm_gb300.solver import BoxSolver
@@ -292,9 +297,11 @@ def main():
         s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
                       inlet_velocity=case["inlet"])
         s.initial_condition()
+        if args.kernel:
+            s.kernel(args.kernel)
         s.step(4)
         s.synchronize()
-        print(json.dumps({"profile_case": args.profile_case, "threads_per_block": s.threads_per_block()}))
+        print(json.dumps({"profile_case": args.profile_case, "threads_per_block": s.threads_per_block(), "kernel": s.kernel()}))
         return
     if args.warmup < 3:
         args.warmup = 3
@@ -424,7 +431,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU", "threads_per_block": tpb,
                    "bulk_kernel": bulk_kernel},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
+                     "traffic": MEASURED_TRAFFIC_PER_STEP.get(args.storage), "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
+                     "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},
         "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + args.steps},
         "variants": variants,
