@@ -119,6 +119,21 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_throughput(local_ms: float, cells_per_rank: int, steps: int, dist=None, device="cuda"):
+    """Replicas: every rank steps its own copy of the workload.  The job time
+    is the slowest rank's (max over ranks); the whole-job MLUPS counts the
+    cells of every rank.  Returns (max_ms, mlups)."""
+    import torch
+
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    world = 1
+    if dist is not None and dist.is_initialized():
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        world = dist.get_world_size()
+    max_ms = float(t.item())
+    return max_ms, cells_per_rank * steps * world / (max_ms / 1e3) / 1e6
+
+
 def cpu_baseline(threads: int, budget_s: float = 12.0):
     """The FP64 CPU restatement (oracle) on a bounded sample of the workload:
     the same geometry scaled to 128 x 64 x 64 cells (sphere radius 6)."""
@@ -263,12 +278,14 @@ def warmstart_run(args):
     rest and from the prediction to residual 1e-8 (per channel)."""
     from lbm_gb300 import warmstart as ws
 
-    out = ws.experiment(n_train=args.ws_train, per_batch=64, train_steps=args.ws_train_steps, epochs=args.ws_epochs, n_eval=16,
-                        per_eval=8, tol=1e-8, max_steps=args.max_steps, log=lambda m: print(m, file=sys.stderr, flush=True))
+    out = ws.experiment(n_train=args.ws_train, per_batch=args.ws_per_batch, train_steps=args.ws_train_steps, epochs=args.ws_epochs,
+                        n_eval=16, per_eval=8, tol=1e-8, max_steps=args.max_steps, lr=args.ws_lr,
+                        log=lambda m: print(m, file=sys.stderr, flush=True))
     return {"metric": "learned warm start: wall time to residual 1e-8, warm / from rest", "value": out["wall_ratio"],
             "unit": "ratio", "higher_is_better": False, "dtype": "f64 (LBM), bf16 (network)",
             "config": {"workload": "D2Q9 forced channel 511x128, 1-8 cylinders r 6-20, Re 20-200, U-Net 4 levels width 32",
-                       "n_train": out["n_train"], "train_steps": out["train_steps"], "epochs": out["epochs"]}, "detail": out}
+                       "n_train": out["n_train"], "train_steps": out["train_steps"], "epochs": out["epochs"],
+                       "per_reynolds_number": args.ws_per_batch}, "detail": out}
 
 
 def main():
@@ -283,8 +300,10 @@ def main():
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
-    ap.add_argument("--ws-train-steps", type=int, default=200000, help="warm start: FP32 steps per training field")
-    ap.add_argument("--ws-epochs", type=int, default=20, help="warm start: training epochs")
+    ap.add_argument("--ws-train-steps", type=int, default=250000, help="warm start: FP32 steps per training field")
+    ap.add_argument("--ws-epochs", type=int, default=60, help="warm start: training epochs")
+    ap.add_argument("--ws-per-batch", type=int, default=32, help="warm start: training channels per Reynolds number")
+    ap.add_argument("--ws-lr", type=float, default=2e-3, help="warm start: peak learning rate")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
@@ -351,11 +370,7 @@ def main():
     with ClockSampler(device) as clk:
         s, tot_ms, ker_ms, launches = run_variant(args.storage, case, args.warmup, args.steps, device)
     barrier()
-    t = torch.tensor([tot_ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    tot_ms = float(t.item())
-    mlups = cells * args.steps * world / (tot_ms / 1e3) / 1e6
+    tot_ms, mlups = job_throughput(tot_ms, cells, args.steps, dist, "cuda")
     kernel_avg_ms = ker_ms / launches
     achieved = B_PER_CELL[args.storage] * cells / (kernel_avg_ms / 1e3) / 1e9
     _, u_head = s.moments()
