@@ -303,7 +303,7 @@ def main():
     ap.add_argument("--ws-train-steps", type=int, default=250000, help="warm start: FP32 steps per training field")
     ap.add_argument("--ws-epochs", type=int, default=60, help="warm start: training epochs")
     ap.add_argument("--ws-per-batch", type=int, default=32, help="warm start: training channels per Reynolds number")
-    ap.add_argument("--ws-lr", type=float, default=2e-3, help="warm start: peak learning rate")
+    ap.add_argument("--ws-lr", type=float, default=1e-3, help="warm start: peak learning rate")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
