@@ -227,6 +227,21 @@ class BoxSolver:
         check(self._lib.lbm_gpu_reduce_mass_momentum(self.ctx, _ptr(out)), self.ctx, "mass_momentum")
         return out
 
+    def write_solution(self, path: str, spacing: float = 1.0) -> str:
+        """The box's moments as the reference's VTK PolyData file, one point
+        per cell at its centre ((i + 1/2) spacing); solid cells included."""
+        from .output import solution_arrays, write_vtp
+
+        nx, ny, nz = self.shape
+        z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        pts = (np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)[:, : max(self.ndim, 2 if nz == 1 else 3)] + 0.5) * spacing
+        rho, u = self.moments()
+        if self.equation == rc.EQ_NAVIER_STOKES:
+            arrays = solution_arrays(self.ndim, rho=rho, u=list(u))
+        else:
+            arrays = solution_arrays(self.ndim, phi=rho)
+        return write_vtp(path, pts, arrays)
+
     def profile_steps(self, n: int):
         """Run n steps with a CUDA event pair around every step-kernel launch;
         returns (device ms of the whole sequence, summed kernel ms, launches)."""
@@ -353,6 +368,21 @@ class LBMSolver:
         self.steps_done = t
         return {"steps": t, "converged": self.converged, "diverged": self.diverged,
                 "residual": None if last_res is None else last_res.tolist()}
+
+    def write_solution(self, path: str) -> str:
+        """``output`` (src/lbm/solver.cpp:322-384): recompute the moments and
+        write the reference's VTK PolyData file (U, V, rho or the potential V
+        at the cell centres)."""
+        from .output import solution_arrays, write_vtp
+
+        self.gpu.update_moments()
+        grid = self.grid
+        v = self.gpu.vars().reshape(grid.ncells, self.consts.nvar)
+        if self.consts.equation == rc.EQ_NAVIER_STOKES:
+            arrays = solution_arrays(grid.ndim, rho=v[:, grid.ndim], u=[v[:, d] for d in range(grid.ndim)])
+        else:
+            arrays = solution_arrays(grid.ndim, phi=v[:, 0])
+        return write_vtp(path, grid.centers.reshape(grid.ncells, grid.ndim), arrays)
 
     def compare_to_analytical(self) -> Dict:
         """``compareToAnalyticalResult`` (src/lbm/solver.cpp:387-482)."""

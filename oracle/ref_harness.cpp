@@ -15,7 +15,11 @@
 // variable, i.e. the number convergenceCondition() would print before the next
 // step.
 //
-// Usage: ref_harness <config.json> <nsteps> <outdir> [--time]
+// With --vtp it also calls the solver's own output(true) at the end, which
+// writes its binary VTK PolyData file (src/lbm/solver.cpp:322-384,
+// src/common/IO.h) into <outdir>: the golden file of the output writer.
+//
+// Usage: ref_harness <config.json> <nsteps> <outdir> [--time] [--vtp]
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -57,7 +61,7 @@ std::string jnum(double x) {
 }
 
 template <LBMethodType LBTYPE, LBEquationType EQ>
-int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const std::string& out, bool timing) {
+int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const std::string& out, bool timing, bool vtp) {
   using S                 = LBMSolver<Debug_Level::no_debug, LBTYPE, EQ>;
   constexpr GInt NDIM     = S::NDIM;
   constexpr GInt NDIST    = S::NDIST;
@@ -163,6 +167,11 @@ int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const st
     meta << "]}";
   }
   meta << "\n  }\n}\n";
+  meta.close();
+  if(vtp) {
+    solver.m_outputDir = out + "/";
+    solver.output(true, "");
+  }
   return 0;
 }
 
@@ -176,7 +185,11 @@ int main(int argc, char** argv) {
   const std::string cfg    = argv[1];
   const long        nsteps = std::stol(argv[2]);
   const std::string out    = argv[3];
-  const bool        timing = argc > 4 && std::string(argv[4]) == "--time";
+  bool              timing = false, vtp = false;
+  for(int a = 4; a < argc; ++a) {
+    timing = timing || std::string(argv[a]) == "--time";
+    vtp    = vtp || std::string(argv[a]) == "--vtp";
+  }
 
   int provided = 0;
   MPI_Init_thread(&argc, &argv, MPI_THREAD_FUNNELED, &provided);
@@ -199,13 +212,13 @@ int main(int argc, char** argv) {
 
   int rc = 1;
   if(model == "D2Q9" && equation == "navierstokes") {
-    rc = runCase<LBMethodType::D2Q9, LBEquationType::Navier_Stokes>(hargc, hargv, cfg, nsteps, out, timing);
+    rc = runCase<LBMethodType::D2Q9, LBEquationType::Navier_Stokes>(hargc, hargv, cfg, nsteps, out, timing, vtp);
   } else if(model == "D2Q9" && equation == "poisson") {
-    rc = runCase<LBMethodType::D2Q9, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing);
+    rc = runCase<LBMethodType::D2Q9, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
   } else if(model == "D2Q5" && equation == "poisson") {
-    rc = runCase<LBMethodType::D2Q5, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing);
+    rc = runCase<LBMethodType::D2Q5, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
   } else if(model == "D1Q3" && equation == "poisson") {
-    rc = runCase<LBMethodType::D1Q3, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing);
+    rc = runCase<LBMethodType::D1Q3, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
   } else {
     std::cerr << "unsupported model/equation " << model << "/" << equation << std::endl;
   }

@@ -7,7 +7,8 @@ Run in a container that has the reference sources (the GPU hosts do not):
 For every case below it runs oracle/_ref/ref_harness (the reference's
 LBMSolver, built from source) for the listed step counts and stores the grid
 tables, the JSON ``solver`` block and the resulting populations, variables and
-residual in tests/golden/<case>_<steps>.npz.  The case configs are either the
+residual in tests/golden/<case>_<steps>.npz (and, for VTP_CASES, the
+reference's own VTK output file).  The case configs are either the
 project's own JSON files in tests/golden/cases/ (written in the reference's
 config schema) or the reference's own test configs, read where they lie.
 """
@@ -81,6 +82,33 @@ def run_case(name, src, steps):
     print(f"{name}_{steps}: {meta['cells']} cells")
 
 
+# cases whose final state the reference also writes through its own VTK
+# output (LBMSolver::output, binary PolyData): tests/golden/<case>_<steps>_ref.vtp
+VTP_CASES = [("cavity_small", 100), ("poisson2d_helmholtz_small", 100)]
+
+
+def run_vtp(name, steps):
+    src = next(s for n, s, _ in CASES if n == name)
+    with open(config_path(src)) as fh:
+        cfg = json.load(fh)
+    with tempfile.TemporaryDirectory() as tmp:
+        local_cfg = os.path.join(tmp, "case.json")
+        with open(local_cfg, "w") as fh:
+            json.dump(cfg, fh)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        subprocess.run([HARNESS, local_cfg, str(steps), out, "--vtp"], cwd=tmp, check=True, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        files = [f for f in os.listdir(out) if f.startswith("solution") and f.endswith(".vtp")]
+        if len(files) != 1:
+            sys.exit(f"{name}: expected one .vtp file, found {files}")
+        with open(os.path.join(out, files[0]), "rb") as fh:
+            data = fh.read()
+    with open(os.path.join(HERE, f"{name}_{steps}_ref.vtp"), "wb") as fh:
+        fh.write(data)
+    print(f"{name}_{steps}_ref.vtp: {len(data)} bytes")
+
+
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
@@ -90,6 +118,10 @@ def main(argv):
             continue
         for n in steps:
             run_case(name, src, n)
+    for name, steps in VTP_CASES:
+        if wanted and name not in wanted:
+            continue
+        run_vtp(name, steps)
 
 
 if __name__ == "__main__":

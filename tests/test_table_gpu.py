@@ -82,3 +82,25 @@ def test_reference_run_loop_converges_on_couette():
     assert res["converged"], res
     cmp = s.compare_to_analytical()
     assert cmp["passed"], cmp
+
+
+@pytest.mark.parametrize("name", ["cavity_small_100", "poisson2d_helmholtz_small_100"])
+def test_solution_output_matches_reference_file(name, tmp_path):
+    """LBMSolver.write_solution after the fixture's steps on the GPU writes
+    the reference's own VTK file (same arrays, bit for bit, same layout)."""
+    import os
+
+    from lbm_gb300.output import read_vtp
+    from lbm_gb300.solver import LBMSolver
+
+    meta, solver, grid, out, consts, bnds, forcing = load_case(name)
+    s = LBMSolver(solver, grid)
+    s.gpu.initial_condition()
+    s.gpu.step(meta["steps"])
+    mine = s.write_solution(str(tmp_path / "solution"))
+    ref = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}_ref.vtp")
+    p0, a0 = read_vtp(ref)
+    p1, a1 = read_vtp(mine)
+    assert np.array_equal(p0, p1) and sorted(a0) == sorted(a1)
+    for k in a0:
+        assert np.array_equal(a0[k], a1[k]), k
