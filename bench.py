@@ -189,6 +189,9 @@ def cavities_run(args):
     steps = b.run(args.cavity_steps, 100, 1e-8, raise_on_divergence=False)
     wall = time.perf_counter() - t0
     status = b.status()
+    res = b.residuals().max(axis=1)
+    ok = np.isfinite(res) & (status != b.DIVERGED)
+    res_q = [float(x) for x in np.percentile(res[ok], [0, 50, 90, 100])] if ok.any() else None
     updates = float(np.sum((steps - before) * area))
     grid, tpb = b.tuning()
     b.close()
@@ -201,7 +204,7 @@ def cavities_run(args):
                          "kernel_avg_ms": kernel_avg_ms},
             "run": {"max_steps": args.cavity_steps, "wall_s": wall, "mlups": updates / wall / 1e6,
                     "converged": int(np.sum(status == b.CONVERGED)), "diverged": int(np.sum(status == b.DIVERGED)),
-                    "of": int(len(area))}}
+                    "of": int(len(area)), "final_residual_min_median_p90_max": res_q}}
 
 
 def poisson_run(args):
