@@ -59,13 +59,22 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
   const int64_t total = P.tile_start[na];
   T*            A     = static_cast<T*>(P.pop);
   const C       lid   = prm<C>(P.lid, P.lid_f);
-  for(int64_t t = warp; t < total; t += nwarps) {
-    int lo = 0, hi = na - 1;  // last active domain whose tiles start at or before t
+  // each warp takes one contiguous run of tiles: the active domain is found
+  // once by binary search and then advances only where the run crosses into
+  // the next domain
+  const int64_t chunk = (total + nwarps - 1) / nwarps;
+  const int64_t t0 = warp * chunk, t1 = t0 + chunk < total ? t0 + chunk : total;
+  int           lo = 0;
+  if(t0 < t1) {
+    int hi = na - 1;  // last active domain whose tiles start at or before t0
     while(lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if(P.tile_start[mid] <= t) lo = mid;
+      if(P.tile_start[mid] <= t0) lo = mid;
       else hi = mid - 1;
     }
+  }
+  for(int64_t t = t0; t < t1; ++t) {
+    while(lo + 1 < na && P.tile_start[lo + 1] <= t) ++lo;
     const BatchDomain D = P.dom[P.active[lo]];
     const int64_t     r = t - P.tile_start[lo];
     const int         y = static_cast<int>(r / D.tiles_per_row);
