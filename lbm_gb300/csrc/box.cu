@@ -851,28 +851,33 @@ void box_destroy(BoxState* b) {
   delete b;
 }
 
-// time one even+odd pair at a given block size (for the autotuner)
+// time one even+odd pair at a given block size (for the autotuner): the
+// fastest of three pairs after two warm-up pairs
 float time_pair(BoxState* b, int tpb, cudaStream_t s) {
   const int keep = b->tuned_tpb;
   b->tuned_tpb   = tpb;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  dispatch_step(b, false, 0, s);
-  dispatch_step(b, true, 0, s);
-  cudaEventRecord(e0, s);
   for(int k = 0; k < 2; ++k) {
     dispatch_step(b, false, 0, s);
     dispatch_step(b, true, 0, s);
   }
-  cudaEventRecord(e1, s);
-  cudaEventSynchronize(e1);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
+  float best = 1e30f;
+  for(int k = 0; k < 3; ++k) {
+    cudaEventRecord(e0, s);
+    dispatch_step(b, false, 0, s);
+    dispatch_step(b, true, 0, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->tuned_tpb = keep;
-  return ms;
+  return best;
 }
 
 // time the even and the odd step separately: the fastest of four of each,
@@ -1120,6 +1125,29 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
         best_odd = od;
         pick_odd = kind;
       }
+    }
+    // the mixed pick only stands if whole step pairs confirm it against the
+    // best single kernel (the parities share the caches and the memory system)
+    if(pick_even != pick_odd) {
+      float best_pair = 1e30f;
+      int   pe = pick_even, po = pick_odd;
+      for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED}) {
+        if(!box_kernel_supported(b, kind)) continue;
+        b->kind_even = b->kind_odd = kind;
+        const float ms = time_pair(b, b->tuned_tpb, stream);
+        if(ms < best_pair) {
+          best_pair = ms;
+          pe = po = kind;
+        }
+      }
+      b->kind_even = pick_even;
+      b->kind_odd  = pick_odd;
+      if(time_pair(b, b->tuned_tpb, stream) < 0.97f * best_pair) {  // a clear margin, or one kernel for both
+        pe = pick_even;
+        po = pick_odd;
+      }
+      pick_even = pe;
+      pick_odd  = po;
     }
     b->kind_even = pick_even;
     b->kind_odd  = pick_odd;

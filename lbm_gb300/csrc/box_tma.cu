@@ -147,7 +147,10 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G    = static_cast<int>(gridDim.x);
-  const int nloc = static_cast<int>(blockIdx.x) < W.nseg ? (W.nseg - 1 - static_cast<int>(blockIdx.x)) / G + 1 : 0;
+  // each CTA takes one contiguous run of segments
+  const int per   = (W.nseg + G - 1) / G;
+  const int first = static_cast<int>(blockIdx.x) * per;
+  const int nloc  = first < W.nseg ? min(per, W.nseg - first) : 0;
   if(threadIdx.x == 0) {
 #pragma unroll
     for(int s = 0; s < NST; ++s) {
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
   const int nx = P.nx, ny = P.ny;
 
   auto coords = [&](int i, int& x0, int& y, int& z) {
-    const uint32_t s  = static_cast<uint32_t>(blockIdx.x) + static_cast<uint32_t>(i) * static_cast<uint32_t>(G);
+    const uint32_t s  = static_cast<uint32_t>(first + i);
     const uint32_t r  = fdiv(s, W.spr);
     const uint32_t zz = fdiv(r, W.nrows);
     x0                = static_cast<int>(s - r * W.spr.d) * kSeg;
@@ -274,7 +277,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
       }
     }
     if constexpr(MOM == 2) {
-      const int64_t s = static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(i) * G;
+      const int64_t s = static_cast<int64_t>(first) + i;
       warp_partials<NV>(diff, P.partials, P.partial_stride, s * kConsumers + (warp - 1));
     }
   }
