@@ -71,21 +71,32 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   bool          work;
   if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
   else work = type != LBM_CELL_SOLID;
-  if(!work) return;
+  // the population loads do not wait for the flag: every address stays inside
+  // the allocation (guard plane in front, ghost plane behind)
   C f[Q];
+  if constexpr(!ODD) {
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      f[q]            = S::load(Ac[q * NA]);
+    });
+  } else {
+    const int sy = P.nx, sz = P.nx * P.ny;
+    static_for<Q>([&](auto qc) {
+      constexpr int q   = decltype(qc)::value;
+      const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+      f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
+    });
+  }
   C mom[NV], prev[NV];
+  prefetch_moments<C, MOM, NV>(P, cell, prev);
+  if(!work) return;
 #pragma unroll
   for(int k = 0; k < NV; ++k) mom[k] = 0;
-  prefetch_moments<C, MOM, NV>(P, cell, prev);
   const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
   if(emit) {
     emit_equilibrium<LAT, EQ, C>(P, f, cell);
   } else {
     if constexpr(!ODD) {
-      static_for<Q>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        f[q]            = S::load(Ac[q * NA]);
-      });
       if(type == LBM_CELL_OUTLET) {
         // links from beyond +x: what the upstream cell received (ghost plane)
         static_for<Q>([&](auto qc) {
@@ -93,13 +104,6 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
           if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
         });
       }
-    } else {
-      const int sy = P.nx, sz = P.nx * P.ny;
-      static_for<Q>([&](auto qc) {
-        constexpr int q   = decltype(qc)::value;
-        const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-        f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
-      });
     }
     collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
   }
@@ -835,7 +839,7 @@ int box_info(const BoxState* b, int64_t* ncells, int32_t* q, int32_t* nvar) {
 void box_destroy(BoxState* b) {
   if(!b) return;
   drop_graphs(b);
-  cudaFree(b->pop);
+  cudaFree(b->pop_alloc);
   cudaFree(b->flags);
   cudaFree(b->dirichlet);
   cudaFree(b->mom);
@@ -1012,8 +1016,13 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
     p.inlet_u_f[d] = static_cast<float>(p.inlet_u[d]);
   }
 
-  cudaError_t e = cudaMalloc(&b->pop, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
-  if(e == cudaSuccess) e = cudaMemset(b->pop, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 1));
+  // one guard plane in front: the odd step issues its pull loads before it
+  // knows whether the cell steps at all, and a boundary cell's pull address
+  // may lie up to nx*ny + nx + 1 cells before plane 0 (behind the last plane
+  // lies the ghost plane)
+  cudaError_t e = cudaMalloc(&b->pop_alloc, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 2));
+  if(e == cudaSuccess) e = cudaMemset(b->pop_alloc, 0, b->elem * static_cast<size_t>(p.nalloc) * (b->Q + 2));
+  b->pop = static_cast<char*>(b->pop_alloc) + b->elem * static_cast<size_t>(p.nalloc);
   // engine bit: a stencil neighbour is solid; and the compact list of cells the
   // odd step must resolve link by link (next to a face or a solid, or not fluid)
   {

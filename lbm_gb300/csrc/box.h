@@ -53,7 +53,8 @@ struct BoxState {
   int          Q = 0, D = 0, nvar = 0;
   int64_t      steps = 0;     // completed steps; parity selects the AA kernel
   size_t       elem  = 8;     // bytes per stored population
-  void*        pop   = nullptr;
+  void*        pop   = nullptr;  // plane 0 of the populations (inside pop_alloc, after one guard plane)
+  void*        pop_alloc = nullptr;  // the allocation: one guard plane, Q planes, the outlet ghost plane
   uint8_t*     flags = nullptr;
   double*      dirichlet = nullptr;
   void*        mom   = nullptr;
