@@ -53,50 +53,29 @@ namespace {
 //   written by the one thread that owns it, so the two kernels may run in
 //   either order.
 // MOM: 0 plain, 1 also write the moments, 2 also accumulate |moments - previous|
-// One cell of the bulk step (the body of k_box_bulk; also the fallback of
-// k_box_pair for pairs that mix cell kinds).  Adds |moment change| to diff.
-template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int z, int cell, uint8_t flag,
-                                          typename Store<ST>::C* diff) {
+// The part of a bulk cell's step after its loads.  SPECIAL = false leaves the
+// inlet / Dirichlet / outlet branches out of the instruction stream (the caller
+// knows that no lane of the warp holds such a cell).
+template <int LAT, int EQ, int ST, bool ODD, int MOM, bool SPECIAL>
+__device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, int cell, uint8_t type, typename Store<ST>::C* f,
+                                            const typename Store<ST>::C* prev, typename Store<ST>::C* diff) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
   constexpr int NV = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
-  const uint8_t type = flag & TYPE_MASK;
   T*            A    = static_cast<T*>(P.pop);
-  T* const      Ac   = A + cell;  // the cell's slot in plane 0
+  T* const      Ac   = A + cell;
   const int     NA   = static_cast<int>(P.nalloc);
-  bool          work;
-  if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
-  else work = type != LBM_CELL_SOLID;
-  // the population loads do not wait for the flag: every address stays inside
-  // the allocation (guard plane in front, ghost plane behind)
-  C f[Q];
-  if constexpr(!ODD) {
-    static_for<Q>([&](auto qc) {
-      constexpr int q = decltype(qc)::value;
-      f[q]            = S::load(Ac[q * NA]);
-    });
-  } else {
-    const int sy = P.nx, sz = P.nx * P.ny;
-    static_for<Q>([&](auto qc) {
-      constexpr int q   = decltype(qc)::value;
-      const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-      f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
-    });
-  }
-  C mom[NV], prev[NV];
-  prefetch_moments<C, MOM, NV>(P, cell, prev);
-  if(!work) return;
+  C             mom[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) mom[k] = 0;
-  const bool emit = !ODD && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+  const bool emit = !ODD && SPECIAL && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
   if(emit) {
     emit_equilibrium<LAT, EQ, C>(P, f, cell);
   } else {
-    if constexpr(!ODD) {
+    if constexpr(!ODD && SPECIAL) {
       if(type == LBM_CELL_OUTLET) {
         // links from beyond +x: what the upstream cell received (ghost plane)
         static_for<Q>([&](auto qc) {
@@ -123,8 +102,56 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   }
 }
 
+// One cell of the bulk step (the body of k_box_bulk; also the fallback of
+// k_box_pair for pairs that mix cell kinds).  Adds |moment change| to diff.
 template <int LAT, int EQ, int ST, bool ODD, int MOM>
-__global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
+__device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int z, int cell, uint8_t flag,
+                                          typename Store<ST>::C* diff) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  constexpr int NV = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
+  const uint8_t type = flag & TYPE_MASK;
+  T* const      Ac   = static_cast<T*>(P.pop) + cell;  // the cell's slot in plane 0
+  const int     NA   = static_cast<int>(P.nalloc);
+  bool          work;
+  if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
+  else work = type != LBM_CELL_SOLID;
+  // the population loads do not wait for the flag: every address stays inside
+  // the allocation (guard plane in front, ghost plane behind)
+  C f[Q];
+  if constexpr(!ODD) {
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      f[q]            = S::load(Ac[q * NA]);
+    });
+  } else {
+    const int sy = P.nx, sz = P.nx * P.ny;
+    static_for<Q>([&](auto qc) {
+      constexpr int q   = decltype(qc)::value;
+      const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
+      f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
+    });
+  }
+  C prev[NV];
+  prefetch_moments<C, MOM, NV>(P, cell, prev);
+  if(!work) return;
+  if constexpr(ODD) {
+    bulk_finish<LAT, EQ, ST, true, MOM, false>(P, y, z, cell, type, f, prev, diff);
+  } else {
+    // one vote per warp: warps of plain fluid (and solid) cells only take the
+    // path without the inlet / Dirichlet / outlet branches.  Each lane votes
+    // for its own cell, so a special cell always takes the full path.
+    const bool special = type != LBM_CELL_FLUID;
+    if(__any_sync(__activemask(), special)) bulk_finish<LAT, EQ, ST, false, MOM, true>(P, y, z, cell, type, f, prev, diff);
+    else bulk_finish<LAT, EQ, ST, false, MOM, false>(P, y, z, cell, type, f, prev, diff);
+  }
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+__device__ __forceinline__ void bulk_grid_cell(const BoxParams& P) {
   using C          = typename Store<ST>::C;
   constexpr int NV = EQ == LBM_NAVIER_STOKES ? Lattice<LAT>::D + 1 : 1;
   const int     x  = blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,6 +168,20 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
     const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
     warp_partials<NV>(diff, P.partials, P.partial_stride, b * (blockDim.x >> 5) + (threadIdx.x >> 5));
   }
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int MOM>
+__global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
+  bulk_grid_cell<LAT, EQ, ST, ODD, MOM>(P);
+}
+
+// The plain step of the FP32 / FP16 / BF16 storages with at most 40 registers
+// per thread: the step is bound by memory latency and instruction issue
+// together, and the extra resident warps hide more of the latency than the
+// compiler's own register choice (48-64 on D3Q19) does.
+template <int LAT, int EQ, int ST, bool ODD>
+__global__ void __maxnreg__(40) k_box_bulk_lean(BoxParams P) {
+  bulk_grid_cell<LAT, EQ, ST, ODD, 0>(P);
 }
 
 // Two populations of adjacent cells as one aligned load / store.
@@ -582,7 +623,10 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     if(staged) {
     } else if(paired) {
       if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, true><<<gp, tpb, 0, s>>>(b->p);
-    } else if(mom == 0) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
+    } else if(mom == 0) {
+      if constexpr(ST == LBM_STORE_F64) k_box_bulk<LAT, EQ, ST, true, 0><<<g, tpb, 0, s>>>(b->p);
+      else k_box_bulk_lean<LAT, EQ, ST, true><<<g, tpb, 0, s>>>(b->p);
+    }
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
     if(nbb) {
@@ -595,7 +639,10 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     if(staged) {
     } else if(paired) {
       if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, false><<<gp, tpb, 0, s>>>(b->p);
-    } else if(mom == 0) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
+    } else if(mom == 0) {
+      if constexpr(ST == LBM_STORE_F64) k_box_bulk<LAT, EQ, ST, false, 0><<<g, tpb, 0, s>>>(b->p);
+      else k_box_bulk_lean<LAT, EQ, ST, false><<<g, tpb, 0, s>>>(b->p);
+    }
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, false, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, false, 2><<<g, tpb, 0, s>>>(b->p);
     if(mom == 2) b->res_slots = nbulk;
