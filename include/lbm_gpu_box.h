@@ -84,6 +84,15 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
  * rho (or phi for Poisson) and ux, uy, uz (NULL to skip). */
 int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, double* uz);
 
+/* Moments of n listed cells of the current state (line probes and other
+ * point samples, the cells of PostprocessCartesianFunctionLine,
+ * src/postprocess/postprocessing_cartesian.h:17-39, whose values
+ * src/postprocess/postprocessing.h:98-115 writes to line.csv): out[i * nvar + k]
+ * with k = 0 rho (phi for Poisson) and k = 1.. the velocity components; the
+ * values equal lbm_gpu_box_moments at those cells bit for bit.  Only the n
+ * cells are read on the device.  LBM_ERR_INVALID for an index outside the box. */
+int lbm_gpu_box_probe(lbm_gpu_ctx* ctx, const int64_t* cells, int64_t n, double* out);
+
 /* Threads per block the autotuner chose for the per-thread step kernel. */
 int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
 /* Bulk step kernel of a box context: LBM_BOX_KERNEL_THREAD (one cell per

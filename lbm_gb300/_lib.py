@@ -74,6 +74,7 @@ _SIGS = {
     "lbm_gpu_destroy": (None, [C.c_void_p]),
     "lbm_gpu_create_box": (C.c_int, [C.POINTER(BoxDesc), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "lbm_gpu_box_moments": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "lbm_gpu_box_probe": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "lbm_gpu_box_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "lbm_gpu_box_select_kernel": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "lbm_gpu_box_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),

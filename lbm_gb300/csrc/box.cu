@@ -407,26 +407,24 @@ __global__ void k_box_outlet(BoxParams P) {
   }
 }
 
-// FP64 post-stream populations of the current state (reference layout of
-// m_fold per cell), q-major, plus inlet/Dirichlet cells reported as the
-// equilibrium they emit and solids as zero
+// FP64 post-stream populations of one cell of the current state (reference
+// layout of m_fold), with inlet/Dirichlet cells reported as the equilibrium
+// they emit and solids as zero; element q goes to out[q * stride]
 template <int LAT, int EQ, int ST>
-__global__ void k_box_readout(BoxParams P, bool odd, double* out) {
+__device__ __forceinline__ void readout_cell(const BoxParams& P, bool odd, int x, int y, int z, double* out, int64_t stride) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
   using C         = typename S::C;
   constexpr int Q = L::Q;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-  if(x >= P.nx) return;
   const int64_t cell = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
   const uint8_t type = P.flags[cell] & TYPE_MASK;
   const T*      A    = static_cast<const T*>(P.pop);
-  const int64_t NA   = P.nalloc, N = P.ncells;
+  const int64_t NA   = P.nalloc;
   C             f[Q];
   if(type == LBM_CELL_SOLID) {
 #pragma unroll
-    for(int q = 0; q < Q; ++q) out[q * N + cell] = 0.0;
+    for(int q = 0; q < Q; ++q) out[q * stride] = 0.0;
     return;
   }
   if(type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET) {
@@ -451,7 +449,15 @@ __global__ void k_box_readout(BoxParams P, bool odd, double* out) {
     }
   }
 #pragma unroll
-  for(int q = 0; q < Q; ++q) out[q * N + cell] = state_to_f<LAT, EQ>(static_cast<double>(f[q]), q);
+  for(int q = 0; q < Q; ++q) out[q * stride] = state_to_f<LAT, EQ>(static_cast<double>(f[q]), q);
+}
+
+template <int LAT, int EQ, int ST>
+__global__ void k_box_readout(BoxParams P, bool odd, double* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if(x >= P.nx) return;
+  const int64_t cell = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
+  readout_cell<LAT, EQ, ST>(P, odd, x, y, z, out + cell, P.ncells);
 }
 
 // store FP64 post-stream populations into the standard (even-parity) layout
@@ -490,34 +496,64 @@ __global__ void k_box_init(BoxParams P, InitVec v) {
 }
 
 // moments (rho or phi, u) of FP64 populations
+// FP64 moments of one cell from its FP64 populations (f[q * stride]):
+// rho and the velocity with the Guo half-force shift, or the potential;
+// written to m[0] (rho or phi) and m[1 + d] (u_d)
 template <int LAT, int EQ>
-__global__ void k_box_moments_f64(BoxParams P, const double* f, double* rho, double* ux, double* uy, double* uz) {
+__device__ __forceinline__ void cell_moments_f64(const BoxParams& P, const double* f, int64_t stride, double* m) {
   using L         = Lattice<LAT>;
   constexpr int Q = L::Q, D = L::D;
-  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if(cell >= P.ncells) return;
-  const int64_t N = P.ncells;
   if constexpr(EQ == LBM_NAVIER_STOKES) {
     double r = 0, j[3] = {0, 0, 0};
 #pragma unroll
     for(int q = 0; q < Q; ++q) {
-      const double v = f[q * N + cell];
+      const double v = f[q * stride];
       r += v;
 #pragma unroll
       for(int d = 0; d < D; ++d) j[d] += L::c(q, d) * v;
     }
     const double F[3] = {P.has_force ? P.force[0] : 0.0, P.has_force ? P.force[1] : 0.0, P.has_force ? P.force[2] : 0.0};
-    if(rho) rho[cell] = r;
-    double* uu[3] = {ux, uy, uz};
+    m[0] = r;
 #pragma unroll
-    for(int d = 0; d < D; ++d)
-      if(uu[d]) uu[d][cell] = r != 0.0 ? (j[d] + 0.5 * F[d]) / r : 0.0;
+    for(int d = 0; d < D; ++d) m[1 + d] = r != 0.0 ? (j[d] + 0.5 * F[d]) / r : 0.0;
   } else {
     double acc = 0;
 #pragma unroll
-    for(int q = 0; q < Q - 1; ++q) acc += f[q * N + cell];
-    if(rho) rho[cell] = acc / (1.0 - L::w(Q - 1));
+    for(int q = 0; q < Q - 1; ++q) acc += f[q * stride];
+    m[0] = acc / (1.0 - L::w(Q - 1));
   }
+}
+
+template <int LAT, int EQ>
+__global__ void k_box_moments_f64(BoxParams P, const double* f, double* rho, double* ux, double* uy, double* uz) {
+  constexpr int D    = Lattice<LAT>::D;
+  const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if(cell >= P.ncells) return;
+  double m[4];
+  cell_moments_f64<LAT, EQ>(P, f + cell, P.ncells, m);
+  if(rho) rho[cell] = m[0];
+  if constexpr(EQ == LBM_NAVIER_STOKES) {
+    double* uu[3] = {ux, uy, uz};
+#pragma unroll
+    for(int d = 0; d < D; ++d)
+      if(uu[d]) uu[d][cell] = m[1 + d];
+  }
+}
+
+// moments of a list of cells (line probes): the same populations and the same
+// arithmetic as the full read-out, for n cells only; out[i * nv + k] with
+// k = 0 rho (phi), 1.. the velocity
+template <int LAT, int EQ, int ST>
+__global__ void k_box_probe(BoxParams P, bool odd, const int64_t* cells, int64_t n, int nv, double* out) {
+  constexpr int Q = Lattice<LAT>::Q;
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if(i >= n) return;
+  const int64_t cell = cells[i];
+  const int64_t row  = cell / P.nx;
+  double        f[Q], m[4];
+  readout_cell<LAT, EQ, ST>(P, odd, static_cast<int>(cell - row * P.nx), static_cast<int>(row % P.ny), static_cast<int>(row / P.ny), f, 1);
+  cell_moments_f64<LAT, EQ>(P, f, 1, m);
+  for(int k = 0; k < nv; ++k) out[i * nv + k] = m[k];
 }
 
 // sum over cells of the FP64 populations: mass and momentum
@@ -659,6 +695,12 @@ cudaError_t launch_readout(BoxState* b, double* out, cudaStream_t s) {
 }
 
 template <int LAT, int EQ, int ST>
+cudaError_t launch_probe(BoxState* b, const int64_t* cells, int64_t n, double* out, cudaStream_t s) {
+  k_box_probe<LAT, EQ, ST><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(b->p, (b->steps & 1) != 0, cells, n, b->nvar, out);
+  return cudaGetLastError();
+}
+
+template <int LAT, int EQ, int ST>
 cudaError_t launch_load(BoxState* b, const double* in, cudaStream_t s) {
   k_box_load<LAT, EQ, ST><<<static_cast<unsigned>((b->p.ncells + 255) / 256), 256, 0, s>>>(b->p, in);
   return cudaGetLastError();
@@ -688,6 +730,9 @@ cudaError_t dispatch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEv
 }
 cudaError_t dispatch_readout(BoxState* b, double* out, cudaStream_t s) { LBM_BOX_DISPATCH(launch_readout, b, out, s); }
 cudaError_t dispatch_load(BoxState* b, const double* in, cudaStream_t s) { LBM_BOX_DISPATCH(launch_load, b, in, s); }
+cudaError_t dispatch_probe(BoxState* b, const int64_t* cells, int64_t n, double* out, cudaStream_t s) {
+  LBM_BOX_DISPATCH(launch_probe, b, cells, n, out, s);
+}
 
 template <int LAT, int EQ, int ST>
 cudaError_t launch_init(BoxState* b, const InitVec& v, cudaStream_t s) {
@@ -1253,6 +1298,33 @@ int lbm_gpu_box_moments(lbm_gpu_ctx* ctx, double* rho, double* ux, double* uy, d
   cudaFree(d);
   if(e != cudaSuccess) {
     lbm_internal_set_error(ctx, std::string("box moments: ") + cudaGetErrorString(e));
+    return LBM_ERR_CUDA;
+  }
+  return LBM_OK;
+}
+
+int lbm_gpu_box_probe(lbm_gpu_ctx* ctx, const int64_t* cells, int64_t n, double* out) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b || n < 0 || (n > 0 && (!cells || !out))) return LBM_ERR_INVALID;
+  if(n == 0) return LBM_OK;
+  for(int64_t i = 0; i < n; ++i)
+    if(cells[i] < 0 || cells[i] >= b->p.ncells) {
+      lbm_internal_set_error(ctx, "box probe: cell index out of range");
+      return LBM_ERR_INVALID;
+    }
+  cudaStream_t s  = lbm_internal_stream(ctx);
+  int64_t*     dc = nullptr;
+  double*      dm = nullptr;
+  cudaError_t  e  = cudaMalloc(&dc, sizeof(int64_t) * n);
+  if(e == cudaSuccess) e = cudaMalloc(&dm, sizeof(double) * n * b->nvar);
+  if(e == cudaSuccess) e = cudaMemcpyAsync(dc, cells, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
+  if(e == cudaSuccess) e = dispatch_probe(b, dc, n, dm, s);
+  if(e == cudaSuccess) e = cudaMemcpyAsync(out, dm, sizeof(double) * n * b->nvar, cudaMemcpyDeviceToHost, s);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(dc);
+  cudaFree(dm);
+  if(e != cudaSuccess) {
+    lbm_internal_set_error(ctx, std::string("box probe: ") + cudaGetErrorString(e));
     return LBM_ERR_CUDA;
   }
   return LBM_OK;

@@ -116,6 +116,107 @@ def solution_arrays(ndim: int, rho: Optional[np.ndarray] = None, u: Optional[Seq
     return [(VEL_NAMES[d], u[d]) for d in range(ndim)] + [("rho", rho)]
 
 
+def line_cells(centers: np.ndarray, half_length, a: Sequence[float], b: Sequence[float]) -> np.ndarray:
+    """The cells a line probe samples (PostprocessCartesianFunctionLine::init,
+    src/postprocess/postprocessing_cartesian.h:17-39): every cell whose centre
+    lies within half a cell length of the line through a and b, ordered by
+    coordinates.
+
+    In 2D the distance is the reference's own: the absolute distance to the
+    hyperplane through a and b (src/common/line.h, Eigen 3.3.91
+    ``Hyperplane<double, 2>::Through``: unit normal (-d_y, d_x) / |d|, offset
+    -a . n, distance |n . p + offset|), evaluated with the same operations in
+    the same order, so cells at exactly half a cell length are decided alike.
+    In 3D that construction is a plane, not a line; here the 3D distance is to
+    the line itself.
+
+    Order: x, then y, then z.  The reference sorts with a comparator that is a
+    strict weak order only when the probe's cells increase in every
+    coordinate together (an axis-parallel line through one row or column of
+    centres, or a line of positive slope); for those lines the two orders
+    agree, for the others the reference's order is unspecified."""
+    c = np.asarray(centers, dtype=np.float64)
+    ndim = c.shape[1]
+    a = np.asarray(a, dtype=np.float64)[:ndim]
+    b = np.asarray(b, dtype=np.float64)[:ndim]
+    d = b - a
+    if ndim == 2:
+        n = np.array([-d[1], d[0]])
+        z = n[0] * n[0] + n[1] * n[1]
+        if z > 0:
+            n = n / np.sqrt(z)
+        off = -(a[0] * n[0] + a[1] * n[1])
+        dist = np.abs((n[0] * c[:, 0] + n[1] * c[:, 1]) + off)
+    else:
+        t = d / np.linalg.norm(d)
+        r = c - a
+        dist = np.linalg.norm(r - np.outer(r @ t, t), axis=1)
+    cells = np.nonzero(np.asarray(half_length) >= dist)[0]
+    keys = tuple(c[cells, k] for k in reversed(range(ndim)))  # lexsort: last key first
+    return cells[np.lexsort(keys)]
+
+
+def box_line_cells(shape, spacing: float, a: Sequence[float], b: Sequence[float]) -> np.ndarray:
+    """line_cells for a dense box of (nx, ny[, nz]) cells of edge `spacing`
+    with centres at (i + 1/2) spacing, without visiting every cell: along the
+    line's dominant axis each layer of cells holds the line's crossing point,
+    and only the cells within two cells of it are tested.  Returns flat cell
+    indices x + nx (y + ny z) in probe order."""
+    nx, ny, nz = (tuple(shape) + (1, 1))[:3]
+    dims = (nx, ny, nz)
+    ndim = 2 if nz == 1 else 3
+    a = np.asarray(a, dtype=np.float64)[:ndim]
+    b = np.asarray(b, dtype=np.float64)[:ndim]
+    d = b - a
+    h = float(spacing)
+    if not np.any(d):
+        cand = np.arange(nx * ny * nz)
+    else:
+        k = int(np.argmax(np.abs(d)))
+        others = [j for j in range(ndim) if j != k]
+        mesh = np.meshgrid(np.arange(dims[k]), *([np.arange(-2, 4)] * len(others)), indexing="ij")
+        t = ((mesh[0] + 0.5) * h - a[k]) / d[k]  # the line's parameter in the layer's mid-plane
+        idx = [None] * ndim
+        idx[k] = mesh[0]
+        for n, j in enumerate(others):
+            idx[j] = np.floor((a[j] + t * d[j]) / h - 0.5).astype(np.int64) + mesh[1 + n]
+        ok = np.ones(mesh[0].shape, dtype=bool)
+        for j in range(ndim):
+            ok &= (idx[j] >= 0) & (idx[j] < dims[j])
+        flat = idx[0] + nx * (idx[1] + (ny * idx[2] if ndim == 3 else 0))
+        cand = np.unique(flat[ok])
+    x = cand % nx
+    y = (cand // nx) % ny
+    z = cand // (nx * ny)
+    centers = (np.stack([x, y, z][:ndim], axis=1) + 0.5) * h
+    return cand[line_cells(centers, 0.5 * h, a, b)]
+
+
+def _g15(v: float) -> str:
+    """A coordinate as the reference's stream prints it (precision 15, default
+    float format: printf's %.15g)."""
+    return "%.15g" % v
+
+
+def write_line_csv(path: str, coords: np.ndarray, values: np.ndarray, name: str = "u") -> str:
+    """The reference's line probe file (ASCII::writePointsCSV,
+    src/common/IO.h:37-88, called from src/postprocess/postprocessing.h:98-115):
+    a header of the coordinate names and the value column, then one row per
+    probe cell with its centre (precision 15) and the value printed with
+    std::fixed and 15 decimals (toStringVector).  `path` gets ".csv" appended
+    if missing (the reference always writes "line.csv")."""
+    if not path.endswith(".csv"):
+        path += ".csv"
+    coords = np.asarray(coords, dtype=np.float64)
+    ndim = coords.shape[1]
+    rows = [",".join(("x", "y", "z")[:ndim]) + "," + name + "\n"]
+    for p, v in zip(coords, np.asarray(values, dtype=np.float64)):
+        rows.append(",".join(_g15(float(x)) for x in p) + "," + ("%.15f" % float(v)) + "\n")
+    with open(path, "w") as fh:
+        fh.write("".join(rows))
+    return path
+
+
 def read_vtp(path: str):
     """Parse a file of this layout (or the reference's): (points (n, 3),
     {name: array}).  For tests and post-processing."""

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -242,6 +243,30 @@ class BoxSolver:
             arrays = solution_arrays(self.ndim, phi=rho)
         return write_vtp(path, pts, arrays)
 
+    def probe(self, cells) -> np.ndarray:
+        """Moments of the listed cells, read on the device for those cells
+        only: (n, nvar) with column 0 rho (phi for Poisson) and 1.. the
+        velocity; equal to moments() at the same cells."""
+        c = np.ascontiguousarray(cells, dtype=np.int64).reshape(-1)
+        out = np.zeros((c.size, self.nvar))
+        check(self._lib.lbm_gpu_box_probe(self.ctx, _ptr(c), int(c.size), _ptr(out)), self.ctx, "probe")
+        return out
+
+    def write_line(self, path: str, a, b, spacing: float = 1.0) -> str:
+        """The reference's line probe (src/postprocess/postprocessing.h:87-119)
+        on the box: the cells within half a cell of the line through a and b
+        (box_line_cells), their centres and the first solution variable (u_x;
+        the potential for Poisson) in the reference's line.csv format."""
+        from .output import box_line_cells, write_line_csv
+
+        cells = box_line_cells(self.shape, spacing, a, b)
+        nx, ny, _ = self.shape
+        ndim = 2 if self.shape[2] == 1 else 3
+        xyz = np.stack([cells % nx, (cells // nx) % ny, cells // (nx * ny)], axis=1)[:, :ndim]
+        m = self.probe(cells)
+        vals = m[:, 1] if self.equation == rc.EQ_NAVIER_STOKES else m[:, 0]
+        return write_line_csv(path, (xyz + 0.5) * spacing, vals)
+
     def profile_steps(self, n: int):
         """Run n steps with a CUDA event pair around every step-kernel launch;
         returns (device ms of the whole sequence, summed kernel ms, launches)."""
@@ -324,6 +349,7 @@ class LBMSolver:
         self.steps_done = 0
         self.converged = False
         self.diverged = False
+        self.output_dir = "."
 
     def run(self, max_steps: Optional[int] = None) -> Dict:
         """The iteration loop of ``LBMSolver::run``: at iteration t the convergence
@@ -338,6 +364,7 @@ class LBMSolver:
         crit = float(cfg.get("convergence", 1e-12))
         g = self.gpu
         g.initial_condition()
+        self._postprocess("atStart")
         t = 0
         last_res = None
         while t < max_steps:
@@ -366,8 +393,28 @@ class LBMSolver:
                 g.step(nxt - t)
                 t = nxt
         self.steps_done = t
+        self._postprocess("atEnd")
         return {"steps": t, "converged": self.converged, "diverged": self.diverged,
                 "residual": None if last_res is None else last_res.tolist()}
+
+    def _postprocess(self, hook: str):
+        """The reference's post-processing objects of this hook
+        (Postprocess::executePostprocess, src/postprocess/postprocessing.h:87-119):
+        each line object writes line.csv into output_dir (the working
+        directory by default, as in the reference; a later object of the same
+        hook overwrites an earlier one there too).  The per-step hooks
+        (beforeTimestep, afterTimestep) are not supported."""
+        pp = self.cfg.get("postprocessing")
+        if not pp:
+            return
+        for name, obj in pp.items():
+            if obj.get("type") != "line":
+                raise ValueError(f"postprocessing {name}: unsupported type {obj.get('type')!r}")
+            ex = obj.get("execute")
+            if ex in ("beforeTimestep", "afterTimestep"):
+                raise NotImplementedError(f"postprocessing {name}: hook {ex} is not supported")
+            if ex == hook:
+                self.write_line(os.path.join(self.output_dir, "line.csv"), obj["A"], obj["B"])
 
     def write_solution(self, path: str) -> str:
         """``output`` (src/lbm/solver.cpp:322-384): recompute the moments and
@@ -383,6 +430,21 @@ class LBMSolver:
         else:
             arrays = solution_arrays(grid.ndim, phi=v[:, 0])
         return write_vtp(path, grid.centers.reshape(grid.ncells, grid.ndim), arrays)
+
+    def write_line(self, path: str, a, b) -> str:
+        """A line probe of the reference's post-processing
+        (src/postprocess/postprocessing.h:87-119, cells from
+        src/postprocess/postprocessing_cartesian.h:17-39): the cells within
+        half a cell length of the line through a and b, their centres and
+        vars(cell, 0), written as the reference's line.csv."""
+        from .output import line_cells, write_line_csv
+
+        grid = self.grid
+        centers = grid.centers.reshape(grid.ncells, grid.ndim)
+        cells = line_cells(centers, 0.5 * grid.cell_length, a, b)
+        self.gpu.update_moments()
+        v = self.gpu.vars().reshape(grid.ncells, self.consts.nvar)
+        return write_line_csv(path, centers[cells], v[cells, 0])
 
     def compare_to_analytical(self) -> Dict:
         """``compareToAnalyticalResult`` (src/lbm/solver.cpp:387-482)."""

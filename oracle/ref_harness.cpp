@@ -19,6 +19,11 @@
 // writes its binary VTK PolyData file (src/lbm/solver.cpp:322-384,
 // src/common/IO.h) into <outdir>: the golden file of the output writer.
 //
+// Like run() (src/lbm/solver.cpp:187, 199) it executes the post-processing
+// hooks atStart and atEnd; a "postprocessing" line object in the case config
+// then writes the reference's line.csv into the working directory
+// (src/postprocess/postprocessing.h:87-119): the golden file of the line probe.
+//
 // Usage: ref_harness <config.json> <nsteps> <outdir> [--time] [--vtp]
 #include <chrono>
 #include <cstdio>
@@ -88,6 +93,7 @@ int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const st
 
   const std::vector<GDouble> fold0 = solver.m_fold;
 
+  solver.executePostprocess(pp::HOOK::ATSTART);
   const auto t0 = std::chrono::steady_clock::now();
   for(long t = 0; t < nsteps; ++t) {
     solver.m_timeStep = t;
@@ -95,6 +101,7 @@ int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const st
     solver.m_currentTime += solver.m_dt;
   }
   const auto   t1      = std::chrono::steady_clock::now();
+  solver.executePostprocess(pp::HOOK::ATEND);
   const double seconds = std::chrono::duration<double>(t1 - t0).count();
 
   const Grid& grid = *static_cast<Grid*>(solver.m_grid.get());

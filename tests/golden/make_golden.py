@@ -109,6 +109,41 @@ def run_vtp(name, steps):
     print(f"{name}_{steps}_ref.vtp: {len(data)} bytes")
 
 
+# line probes (the reference's "postprocessing" line objects, executed at the
+# end of the run, src/postprocess/postprocessing.h:87-119): the reference's own
+# line.csv after <steps> steps -> tests/golden/<case>_<steps>_line_<tag>.csv.
+# Lines run through cell centres along an axis or with a positive slope: there
+# the reference's sort comparator is a strict weak order, so its cell order is
+# defined.
+LINE_CASES = [
+    ("cavity_small", 100, "x0p53", [0.53125, 0.0], [0.53125, 1.0]),
+    ("cavity_small", 100, "diag", [0.0, 0.0], [1.0, 1.0]),
+    ("poisson2d_helmholtz_small", 100, "y0p41", [0.0, 0.40625], [1.0, 0.40625]),
+    ("channel_mixed_small", 100, "x1p06", [1.0625, 0.0], [1.0625, 1.0]),
+]
+
+
+def run_line(name, steps, tag, a, b):
+    src = next(s for n, s, _ in CASES if n == name)
+    with open(config_path(src)) as fh:
+        cfg = json.load(fh)
+    cfg["solver"]["postprocessing"] = {"line1": {"type": "line", "execute": "atEnd", "A": a, "B": b}}
+    with tempfile.TemporaryDirectory() as tmp:
+        local_cfg = os.path.join(tmp, "case.json")
+        with open(local_cfg, "w") as fh:
+            json.dump(cfg, fh)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        subprocess.run([HARNESS, local_cfg, str(steps), out], cwd=tmp, check=True, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        with open(os.path.join(tmp, "line.csv"), "rb") as fh:
+            data = fh.read()
+    dst = os.path.join(HERE, f"{name}_{steps}_line_{tag}.csv")
+    with open(dst, "wb") as fh:
+        fh.write(data)
+    print(f"{os.path.basename(dst)}: {data.count(b'\n') - 1} points")
+
+
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
@@ -122,6 +157,10 @@ def main(argv):
         if wanted and name not in wanted:
             continue
         run_vtp(name, steps)
+    for name, steps, tag, a, b in LINE_CASES:
+        if wanted and name not in wanted:
+            continue
+        run_line(name, steps, tag, a, b)
 
 
 if __name__ == "__main__":

@@ -230,3 +230,45 @@ def test_stacked_2d_slices_evolve_independently():
     s1.initial_condition()
     s1.step(41)
     assert np.array_equal(s1.populations(), f[:, n1:2 * n1])
+
+
+@pytest.mark.parametrize("case,storage", [("d3q19_sphere_open", "f16dev"), ("d3q19_sphere_open", "f64"), ("d2q9_open_cylinder", "f32"),
+                                          ("d3q19_lid", "f64")])
+@pytest.mark.parametrize("steps", [6, 7])
+def test_probe_equals_moments_bitwise(case, storage, steps):
+    """lbm_gpu_box_probe reads only the listed cells on the device and gives
+    exactly lbm_gpu_box_moments' values there (both parities of the AA step,
+    inlet / outlet / solid cells included)."""
+    g, _ = make_pair(case, storage)
+    g.initial_condition()
+    g.step(steps)
+    rho, u = g.moments()
+    rng = np.random.default_rng(steps)
+    cells = np.concatenate([[0, g.ncells - 1], rng.integers(0, g.ncells, 200)])
+    m = g.probe(cells)
+    assert np.array_equal(m[:, 0], rho[cells])
+    for d in range(g.ndim):
+        assert np.array_equal(m[:, 1 + d], u[d][cells])
+    with pytest.raises(Exception):
+        g.probe([g.ncells])
+
+
+@pytest.mark.parametrize("case", ["d3q19_sphere_open", "d2q9_open_cylinder"])
+def test_box_line_probe_file(case, tmp_path):
+    """write_line on the box: the probe cells' centres and u_x, in the
+    reference's line.csv format, agree with the full moment read-out."""
+    from lbm_gb300.output import box_line_cells
+
+    g, _ = make_pair(case, "f64")
+    g.initial_condition()
+    g.step(9)
+    _, u = g.moments()
+    nx, ny, nz = g.shape
+    # 3D: along x through a row of cell centres; 2D: a slanted line
+    a, b = ([0.0, ny // 2 + 0.5, nz // 2 + 0.5], [nx, ny // 2 + 0.5, nz // 2 + 0.5]) if nz > 1 else ([nx / 3.0, 0.0], [nx / 3.0 + 2.0, ny])
+    path = g.write_line(str(tmp_path / "line"), a, b, spacing=1.0)
+    cells = box_line_cells(g.shape, 1.0, a, b)
+    rows = open(path).read().splitlines()
+    assert rows[0] == ("x,y,z,u" if nz > 1 else "x,y,u") and len(rows) == 1 + cells.size > 1
+    vals = np.array([float(r.split(",")[-1]) for r in rows[1:]])
+    assert np.allclose(vals, u[0][cells], rtol=0, atol=5e-16)

@@ -70,3 +70,73 @@ def test_matches_reference_vtk_output(name, tmp_path):
     for k in a0:
         assert np.array_equal(a0[k], a1[k]), k
     assert _tags(open(ref).read()) == _tags(open(mine).read())
+
+
+# ---- line probes (the reference's post-processing line.csv) -----------------
+
+LINES = [
+    ("cavity_small", 100, "x0p53", [0.53125, 0.0], [0.53125, 1.0]),
+    ("cavity_small", 100, "diag", [0.0, 0.0], [1.0, 1.0]),
+    ("poisson2d_helmholtz_small", 100, "y0p41", [0.0, 0.40625], [1.0, 0.40625]),
+    ("channel_mixed_small", 100, "x1p06", [1.0625, 0.0], [1.0625, 1.0]),
+]
+
+
+@pytest.mark.parametrize("name,steps,tag,a,b", LINES)
+def test_line_probe_matches_reference_file(name, steps, tag, a, b, tmp_path):
+    """Cell selection, order and formatting of the line probe against the
+    reference's own line.csv for the same state: the fixture's vars after the
+    steps (the reference's m_vars) through line_cells and write_line_csv give
+    the reference's file byte for byte."""
+    import json
+
+    from lbm_gb300.output import line_cells, write_line_csv
+
+    d = np.load(os.path.join(GOLD, f"{name}_{steps}.npz"))
+    meta = json.loads(str(d["meta"]))
+    centers = d["centers"].reshape(-1, meta["ndim"])
+    v = d["vars"].reshape(-1, meta["nvar"])
+    cells = line_cells(centers, 0.5 * meta["cellLength"], a, b)
+    mine = write_line_csv(str(tmp_path / "line"), centers[cells], v[cells, 0])
+    with open(mine) as fh, open(os.path.join(GOLD, f"{name}_{steps}_line_{tag}.csv")) as gh:
+        assert fh.read() == gh.read()
+
+
+def _brute_line(shape, h, a, b):
+    from lbm_gb300.output import line_cells
+
+    nx, ny, nz = (tuple(shape) + (1, 1))[:3]
+    nd = 2 if nz == 1 else 3
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    cent = (np.stack([x.ravel(), y.ravel(), z.ravel()], 1)[:, :nd] + 0.5) * h
+    return line_cells(cent, 0.5 * h, a, b)
+
+
+def test_box_line_cells_match_a_scan_of_every_cell():
+    """box_line_cells (a few cells per layer along the line) selects and
+    orders exactly what testing every cell of the box selects."""
+    from lbm_gb300.output import box_line_cells
+
+    rng = np.random.default_rng(3)
+    for trial in range(120):
+        nd = 2 + trial % 2
+        shape = tuple(int(v) for v in rng.integers(3, 12, size=nd)) + (1,) * (3 - nd)
+        h = float(rng.choice([1.0, 0.25]))
+        ext = np.array(shape[:nd]) * h
+        a = rng.uniform(-0.5, 1.5, nd) * ext
+        b = rng.uniform(-0.5, 1.5, nd) * ext
+        if trial % 4 == 0:  # axis-parallel through cell centres
+            a = (np.floor(a / h) + 0.5) * h
+            b = a.copy()
+            b[trial % nd] += 3 * h
+        assert np.array_equal(box_line_cells(shape, h, a, b), _brute_line(shape, h, a, b)), (trial, shape, a, b)
+
+
+def test_line_csv_format(tmp_path):
+    """Header of coordinate names and 'u'; coordinates at precision 15 in the
+    shortest form, values in fixed notation with 15 decimals."""
+    from lbm_gb300.output import write_line_csv
+
+    p = write_line_csv(str(tmp_path / "l"), np.array([[0.03125, 1.0 / 3.0], [2.5, 1e-7]]), np.array([-1.0 / 3.0, 5e-17]))
+    with open(p) as fh:
+        assert fh.read() == "x,y,u\n0.03125,0.333333333333333,-0.333333333333333\n2.5,1e-07,0.000000000000000\n"

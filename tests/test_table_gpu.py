@@ -104,3 +104,42 @@ def test_solution_output_matches_reference_file(name, tmp_path):
     assert np.array_equal(p0, p1) and sorted(a0) == sorted(a1)
     for k in a0:
         assert np.array_equal(a0[k], a1[k]), k
+
+
+LINES = [
+    ("cavity_small", 100, "x0p53", [0.53125, 0.0], [0.53125, 1.0]),
+    ("cavity_small", 100, "diag", [0.0, 0.0], [1.0, 1.0]),
+    ("poisson2d_helmholtz_small", 100, "y0p41", [0.0, 0.40625], [1.0, 0.40625]),
+    ("channel_mixed_small", 100, "x1p06", [1.0625, 0.0], [1.0625, 1.0]),
+]
+
+
+@pytest.mark.parametrize("name,steps,tag,a,b", LINES)
+def test_line_probe_matches_reference_file(name, steps, tag, a, b, tmp_path):
+    """The reference's post-processing line probe after the fixture's steps on
+    the GPU: LBMSolver.write_line writes the reference's own line.csv byte for
+    byte; run() with the line in the config's "postprocessing" (executed
+    atEnd) writes the same file."""
+    import copy
+    import os
+
+    from lbm_gb300.solver import LBMSolver
+
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}_{steps}_line_{tag}.csv")
+    with open(gold) as fh:
+        ref = fh.read()
+    meta, solver, grid, out, consts, bnds, forcing = load_case(f"{name}_{steps}")
+    s = LBMSolver(solver, grid)
+    s.gpu.initial_condition()
+    s.gpu.step(meta["steps"])
+    with open(s.write_line(str(tmp_path / "line"), a, b)) as fh:
+        assert fh.read() == ref
+    cfg = copy.deepcopy(solver)
+    cfg["postprocessing"] = {"line1": {"type": "line", "execute": "atEnd", "A": a, "B": b}}
+    cfg["convergence"] = 0.0
+    r = LBMSolver(cfg, grid)
+    r.output_dir = str(tmp_path)
+    res = r.run(max_steps=steps)
+    assert res["steps"] == steps
+    with open(tmp_path / "line.csv") as fh:
+        assert fh.read() == ref
