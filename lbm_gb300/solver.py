@@ -436,13 +436,15 @@ class LBMSolver:
         (src/postprocess/postprocessing.h:87-119, cells from
         src/postprocess/postprocessing_cartesian.h:17-39): the cells within
         half a cell length of the line through a and b, their centres and
-        vars(cell, 0), written as the reference's line.csv."""
+        vars(cell, 0), written as the reference's line.csv.  Like the
+        reference it reports the variables as they stand (the ones the last
+        step computed, or the last output's update); it does not recompute
+        them."""
         from .output import line_cells, write_line_csv
 
         grid = self.grid
         centers = grid.centers.reshape(grid.ncells, grid.ndim)
         cells = line_cells(centers, 0.5 * grid.cell_length, a, b)
-        self.gpu.update_moments()
         v = self.gpu.vars().reshape(grid.ncells, self.consts.nvar)
         return write_line_csv(path, centers[cells], v[cells, 0])
 
