@@ -471,10 +471,14 @@ __global__ void k_box_load(BoxParams P, const double* in) {
   const int64_t cell = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if(cell >= P.ncells) return;
   T* A = static_cast<T*>(P.pop);
+  // every load before the first store (a load after a store the compiler
+  // cannot prove disjoint would wait for it); `in` may be host memory read
+  // over the CPU-GPU link, where a round trip per direction would be slow
+  double v[Q];
 #pragma unroll
-  for(int q = 0; q < Q; ++q) {
-    A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(in[q * P.ncells + cell], q)));
-  }
+  for(int q = 0; q < Q; ++q) v[q] = in[q * P.ncells + cell];
+#pragma unroll
+  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(v[q], q)));
 }
 
 // uniform initial state: the same FP64 population vector in every cell
@@ -887,13 +891,33 @@ int box_get_populations(BoxState* b, double* f, cudaStream_t s, std::string& err
   return e == cudaSuccess ? LBM_OK : cerr(err, e, "get populations");
 }
 
-int box_set_populations(BoxState* b, const double* f, cudaStream_t s, std::string& err) {
-  if(!ensure_staging(b)) {
-    err = "staging allocation failed";
-    return LBM_ERR_NOMEM;
+// A host array the device can read in place: page-locked memory mapped into
+// the device's address space (on Grace-Blackwell the load kernel then streams
+// it over the coherent CPU-GPU link and converts on the fly, with no staging
+// copy); nullptr for anything else.
+static const double* device_view_of_host(const double* f) {
+  cudaPointerAttributes a{};
+  if(cudaPointerGetAttributes(&a, f) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory of an older driver: clear the error
+    return nullptr;
   }
-  cudaError_t e = cudaMemcpyAsync(b->f64, f, sizeof(double) * b->Q * b->p.ncells, cudaMemcpyHostToDevice, s);
-  if(e == cudaSuccess) e = dispatch_load(b, b->f64, s);
+  if(a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return static_cast<const double*>(a.devicePointer);
+}
+
+int box_set_populations(BoxState* b, const double* f, cudaStream_t s, std::string& err) {
+  cudaError_t   e      = cudaSuccess;
+  const double* direct = device_view_of_host(f);
+  if(direct) {
+    e = dispatch_load(b, direct, s);
+  } else {
+    if(!ensure_staging(b)) {
+      err = "staging allocation failed";
+      return LBM_ERR_NOMEM;
+    }
+    e = cudaMemcpyAsync(b->f64, f, sizeof(double) * b->Q * b->p.ncells, cudaMemcpyHostToDevice, s);
+    if(e == cudaSuccess) e = dispatch_load(b, b->f64, s);
+  }
   if(e == cudaSuccess) e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return cerr(err, e, "set populations");
   b->steps     = 0;  // the layout is now the even-parity (standard) one
