@@ -56,9 +56,13 @@ namespace {
 // The part of a bulk cell's step after its loads.  SPECIAL = false leaves the
 // inlet / Dirichlet / outlet branches out of the instruction stream (the caller
 // knows that no lane of the warp holds such a cell).
-template <int LAT, int EQ, int ST, bool ODD, int MOM, bool SPECIAL>
+// XFP (odd step): some lane of the warp holds an XFACE cell (xf for this
+// lane): an inlet emits its equilibrium, an outlet pulls its c_x < 0 links from
+// the ghost plane, and neither pushes through its open face.
+template <int LAT, int EQ, int ST, bool ODD, int MOM, bool SPECIAL, bool XFP = false>
 __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, int cell, uint8_t type, typename Store<ST>::C* f,
-                                            const typename Store<ST>::C* prev, typename Store<ST>::C* diff) {
+                                            const typename Store<ST>::C* prev, typename Store<ST>::C* diff, bool xf = false,
+                                            int x = 0) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -71,10 +75,20 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
   C             mom[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) mom[k] = 0;
-  const bool emit = !ODD && SPECIAL && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+  const bool emit = (!ODD && SPECIAL && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET)) ||
+                    (ODD && XFP && xf && type == LBM_CELL_INLET);
   if(emit) {
     emit_equilibrium<LAT, EQ, C>(P, f, cell);
   } else {
+    if constexpr(ODD && XFP) {
+      if(xf) {
+        // the outlet: links from beyond +x, the ghost plane
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+        });
+      }
+    }
     if constexpr(!ODD && SPECIAL) {
       if(type == LBM_CELL_OUTLET) {
         // links from beyond +x: what the upstream cell received (ghost plane)
@@ -93,18 +107,26 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
       Ac[L::opp(q) * NA] = S::store(f[q]);
     });
   } else {
-    const int sy = P.nx, sz = P.nx * P.ny;
+    const int  sy = P.nx, sz = P.nx * P.ny;
+    const bool drop_neg = XFP && xf && x == 0;          // the inlet: nothing leaves through -x
+    const bool drop_pos = XFP && xf && x == P.nx - 1;   // the outlet: nothing leaves through +x
     static_for<Q>([&](auto qc) {
       constexpr int q   = decltype(qc)::value;
       const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-      Ac[q * NA + off]  = S::store(f[q]);
+      if constexpr(XFP && L::c(q, 0) < 0) {
+        if(drop_neg) return;
+      }
+      if constexpr(XFP && L::c(q, 0) > 0) {
+        if(drop_pos) return;
+      }
+      Ac[q * NA + off] = S::store(f[q]);
     });
   }
 }
 
 // One cell of the bulk step (the body of k_box_bulk; also the fallback of
 // k_box_pair for pairs that mix cell kinds).  Adds |moment change| to diff.
-template <int LAT, int EQ, int ST, bool ODD, int MOM>
+template <int LAT, int EQ, int ST, bool ODD, int MOM, bool XF = false>
 __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int z, int cell, uint8_t flag,
                                           typename Store<ST>::C* diff) {
   using L         = Lattice<LAT>;
@@ -117,7 +139,8 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   T* const      Ac   = static_cast<T*>(P.pop) + cell;  // the cell's slot in plane 0
   const int     NA   = static_cast<int>(P.nalloc);
   bool          work;
-  if constexpr(ODD) work = flag == LBM_CELL_FLUID;  // fluid, and not LINKED
+  const bool    xf = ODD && XF && (flag & XFACE);
+  if constexpr(ODD) work = flag == LBM_CELL_FLUID || xf;  // fluid and not LINKED, or stepped in line
   else work = type != LBM_CELL_SOLID;
   // the population loads do not wait for the flag: every address stays inside
   // the allocation (guard plane in front, ghost plane behind)
@@ -139,6 +162,12 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   prefetch_moments<C, MOM, NV>(P, cell, prev);
   if(!work) return;
   if constexpr(ODD) {
+    if constexpr(XF) {
+      if(__any_sync(__activemask(), xf)) {
+        bulk_finish<LAT, EQ, ST, true, MOM, false, true>(P, y, z, cell, type, f, prev, diff, xf, x);
+        return;
+      }
+    }
     bulk_finish<LAT, EQ, ST, true, MOM, false>(P, y, z, cell, type, f, prev, diff);
   } else {
     // one vote per warp: warps of plain fluid (and solid) cells only take the
@@ -162,7 +191,7 @@ __device__ __forceinline__ void bulk_grid_cell(const BoxParams& P) {
   for(int k = 0; k < NV; ++k) diff[k] = C(0);
   if(x < P.nx) {
     const int cell = x + P.nx * (y + P.ny * z);
-    bulk_cell<LAT, EQ, ST, ODD, MOM>(P, x, y, z, cell, P.flags[cell], diff);
+    bulk_cell<LAT, EQ, ST, ODD, MOM, true>(P, x, y, z, cell, P.flags[cell], diff);
   }
   if constexpr(MOM == 2) {
     const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
@@ -323,7 +352,7 @@ __global__ void k_box_build_links(BoxParams P, const int32_t* list, int n, int32
 }
 
 template <int LAT, int EQ, int ST, int MOM>
-__global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int n, int64_t slot0, const int32_t* src,
+__global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int count, int n, int64_t slot0, const int32_t* src,
                                                  const int32_t* dst, const double* corr_src, const double* corr_dst) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
@@ -335,7 +364,7 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
   C             diff[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) diff[k] = C(0);
-  if(i < n) {
+  if(i < count) {  // the first `count` entries; tables have stride n
     const int     cell = list[i];
     const uint8_t type = P.flags[cell] & TYPE_MASK;
     T*            A    = static_cast<T*>(P.pop);
@@ -650,10 +679,13 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   }
   if(ev0) cudaEventRecord(ev0, s);
   int64_t        nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel
-  const unsigned nbb   = static_cast<unsigned>((b->n_bnd + 127) / 128);
   const int      kind   = odd ? b->kind_odd : b->kind_even;
   const bool     staged = kind == LBM_BOX_KERNEL_STAGED;
   const bool     paired = kind == LBM_BOX_KERNEL_PAIRED && mom == 0;  // residual steps use the per-thread kernel
+  // the per-thread odd kernel steps the XFACE cells itself; with the others the
+  // boundary kernel takes them too (they close its list)
+  const int      nlist  = static_cast<int>(staged || paired ? b->n_bnd : b->n_bnd_lean);
+  const unsigned nbb    = static_cast<unsigned>((nlist + 127) / 128);
   const dim3     gp(static_cast<unsigned>((b->p.nx / 2 + tpb - 1) / tpb), static_cast<unsigned>(b->p.ny), static_cast<unsigned>(b->p.nz));
   if(staged) {
     const cudaError_t e = box_tma_bulk(b, odd, mom, s, &nbulk);
@@ -670,9 +702,9 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
     if(nbb) {
-      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
-      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
-      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
     }
     if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
@@ -1143,7 +1175,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   // odd step must resolve link by link (next to a face or a solid, or not fluid)
   {
     const int nx = desc->nx, ny = desc->ny, nz = desc->nz;
-    std::vector<int32_t> list;
+    std::vector<int32_t> list, xlist;
     for(int64_t i = 0; i < ncells; ++i) {
       const int x = static_cast<int>(i % nx), y = static_cast<int>((i / nx) % ny), z = static_cast<int>(i / (static_cast<int64_t>(nx) * ny));
       if(hflags[i] == LBM_CELL_SOLID) continue;
@@ -1156,10 +1188,21 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
             if(xx < 0 || yy < 0 || zz < 0 || xx >= nx || yy >= ny || zz >= nz) continue;
             if(hflags[xx + static_cast<int64_t>(nx) * (yy + static_cast<int64_t>(ny) * zz)] == LBM_CELL_SOLID) near = true;
           }
-      const bool inside = x > 0 && x < nx - 1 && y > 0 && y < ny - 1 && (D < 3 || (z > 0 && z < nz - 1));
+      const bool inside_yz = y > 0 && y < ny - 1 && (D < 3 || (z > 0 && z < nz - 1));
+      const bool inside    = x > 0 && x < nx - 1 && inside_yz;
+      const bool xface     = !near && inside_yz && nx >= 3 &&
+                         ((x == 0 && hflags[i] == LBM_CELL_INLET && desc->face[0] == LBM_FACE_OPEN) ||
+                          (x == nx - 1 && hflags[i] == LBM_CELL_OUTLET && desc->face[1] == LBM_FACE_OPEN));
+      if(xface) {
+        xlist.push_back(static_cast<int32_t>(i));
+        hflags[i] = static_cast<uint8_t>(hflags[i] | XFACE);
+        continue;
+      }
       if(near || !inside || hflags[i] != LBM_CELL_FLUID) list.push_back(static_cast<int32_t>(i));
       if(near || !inside) hflags[i] = static_cast<uint8_t>(hflags[i] | LINKED);
     }
+    b->n_bnd_lean = static_cast<int64_t>(list.size());
+    list.insert(list.end(), xlist.begin(), xlist.end());
     b->n_bnd = static_cast<int64_t>(list.size());
     if(e == cudaSuccess) e = cudaMalloc(&b->bnd_list, sizeof(int32_t) * std::max<size_t>(1, list.size()));
     if(e == cudaSuccess && !list.empty())

@@ -66,8 +66,9 @@ struct BoxState {
   int          res_ready = 0;  // partials hold the residual of the last step
   int          mom_valid = 0;  // mom holds the moments of the last step
   int          tuned_tpb = 128;
-  int32_t*     bnd_list  = nullptr;  // cells the odd step resolves link by link
+  int32_t*     bnd_list  = nullptr;  // cells the odd step resolves link by link; XFACE cells last
   int64_t      n_bnd     = 0;
+  int64_t      n_bnd_lean = 0;       // leading entries without the XFACE cells (per-thread odd kernel)
   int32_t*     link_src  = nullptr;  // n_bnd x Q pull slots of the boundary cells
   int32_t*     link_dst  = nullptr;  // n_bnd x Q push slots (-1: leaves the box)
   double*      corr_src  = nullptr;  // moving-wall terms (allocated only when a wall moves)

@@ -17,6 +17,11 @@ namespace lbm {
 constexpr uint8_t TYPE_MASK  = 0x07;
 constexpr uint8_t LINKED     = 0x08;  // set by the engine: the odd step resolves this cell's links in the
                                      // boundary kernel (a solid neighbour, or a face of the box)
+constexpr uint8_t XFACE      = 0x10;  // set by the engine: an inlet cell on an open -x face or an outlet
+                                     // cell on an open +x face, away from solids and the other faces; the
+                                     // per-thread odd step handles it in line (emit, or ghost pulls, and
+                                     // no push through the face), the other bulk kernels leave it to the
+                                     // boundary kernel
 // ---- link resolution ---------------------------------------------------------
 // mirror of direction q in the axes of `mask` (free-slip reflection)
 template <int LAT>

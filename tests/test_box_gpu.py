@@ -126,8 +126,12 @@ def test_bulk_kernels_agree_bitwise(case, storage, other):
         a.step(n)
         b.step(n)
         assert np.array_equal(a.populations(), b.populations()), n
-    # same moment changes, summed over differently shaped partial slots
-    np.testing.assert_allclose(a.residual(), b.residual(), rtol=1e-12, atol=0)
+    # same moment changes, summed over differently shaped partial slots; the
+    # reduced-precision storages compute in FP32 and form FP32 per-warp
+    # partials, so a cell that lands in another warp's partial changes the
+    # rounding at the FP32 level
+    rtol = 1e-12 if storage == "f64" else 1e-6
+    np.testing.assert_allclose(a.residual(), b.residual(), rtol=rtol, atol=0)
 
 
 @pytest.mark.parametrize("case", ["d3q19_sphere_open", "d2q9_guo_channel"])
