@@ -56,13 +56,18 @@ namespace {
 // The part of a bulk cell's step after its loads.  SPECIAL = false leaves the
 // inlet / Dirichlet / outlet branches out of the instruction stream (the caller
 // knows that no lane of the warp holds such a cell).
-// XFP (odd step): some lane of the warp holds an XFACE cell (xf for this
-// lane): an inlet emits its equilibrium, an outlet pulls its c_x < 0 links from
-// the ghost plane, and neither pushes through its open face.
+// XFP (odd step): some lane of the warp holds an XFACE or SFACE cell (xf, sf
+// for this lane).  XFACE: an inlet emits its equilibrium, an outlet pulls its
+// c_x < 0 links from the ghost plane, and neither pushes through its open
+// face.  SFACE: the links through the free-slip face are reflected in it (the
+// population arriving in direction q comes from the face neighbour x - c_q
+// projected on the face, in the mirrored direction; a population leaving
+// through the face lands mirrored on x + c_q projected on the face), as
+// resolve() gives for the boundary kernel's link tables.
 template <int LAT, int EQ, int ST, bool ODD, int MOM, bool SPECIAL, bool XFP = false>
 __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, int cell, uint8_t type, typename Store<ST>::C* f,
                                             const typename Store<ST>::C* prev, typename Store<ST>::C* diff, bool xf = false,
-                                            int x = 0) {
+                                            int x = 0, bool sf = false) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -77,6 +82,10 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
   for(int k = 0; k < NV; ++k) mom[k] = 0;
   const bool emit = (!ODD && SPECIAL && (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET)) ||
                     (ODD && XFP && xf && type == LBM_CELL_INLET);
+  // SFACE: the c_y (c_z) whose pull crosses the cell's free-slip face, 0 if
+  // none (formed where it is used, so nothing extra lives across the collision)
+  const auto pull_y = [&]() { return (L::D > 1 && sf) ? (y == 0 ? 1 : (y == P.ny - 1 ? -1 : 0)) : 0; };
+  const auto pull_z = [&]() { return (L::D > 2 && sf) ? (z == 0 ? 1 : (z == P.nz - 1 ? -1 : 0)) : 0; };
   if(emit) {
     emit_equilibrium<LAT, EQ, C>(P, f, cell);
   } else {
@@ -86,6 +95,22 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
           if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+        });
+      }
+      if(sf) {
+        // links through the free-slip face: the mirrored population of the
+        // face neighbour (inside the box: the cell is not on an x face or a
+        // second y / z face)
+        const int sy = P.nx, sz = P.nx * P.ny;
+        const int py = pull_y(), pz = pull_z();
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          if constexpr(L::D > 1 && L::c(q, 1) != 0) {
+            if(L::c(q, 1) == py) f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 1>(q)) * NA - (L::c(q, 0) + sz * L::c(q, 2))]);
+          }
+          if constexpr(L::D > 2 && L::c(q, 2) != 0) {
+            if(L::c(q, 2) == pz) f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 2>(q)) * NA - (L::c(q, 0) + sy * L::c(q, 1))]);
+          }
         });
       }
     }
@@ -110,6 +135,7 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
     const int  sy = P.nx, sz = P.nx * P.ny;
     const bool drop_neg = XFP && xf && x == 0;          // the inlet: nothing leaves through -x
     const bool drop_pos = XFP && xf && x == P.nx - 1;   // the outlet: nothing leaves through +x
+    const int  py = XFP ? pull_y() : 0, pz = XFP ? pull_z() : 0;
     static_for<Q>([&](auto qc) {
       constexpr int q   = decltype(qc)::value;
       const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
@@ -119,6 +145,18 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
       if constexpr(XFP && L::c(q, 0) > 0) {
         if(drop_pos) return;
       }
+      if constexpr(XFP && L::D > 1 && L::c(q, 1) != 0) {
+        if(L::c(q, 1) == -py) {  // leaves through the free-slip face: lands mirrored on the face
+          Ac[mirror_axis<LAT, 1>(q) * NA + L::c(q, 0) + sz * L::c(q, 2)] = S::store(f[q]);
+          return;
+        }
+      }
+      if constexpr(XFP && L::D > 2 && L::c(q, 2) != 0) {
+        if(L::c(q, 2) == -pz) {
+          Ac[mirror_axis<LAT, 2>(q) * NA + L::c(q, 0) + sy * L::c(q, 1)] = S::store(f[q]);
+          return;
+        }
+      }
       Ac[q * NA + off] = S::store(f[q]);
     });
   }
@@ -126,7 +164,11 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
 
 // One cell of the bulk step (the body of k_box_bulk; also the fallback of
 // k_box_pair for pairs that mix cell kinds).  Adds |moment change| to diff.
-template <int LAT, int EQ, int ST, bool ODD, int MOM, bool XF = false>
+// XF (odd step): 0 plain; 1 the bulk kernel, which also steps the XFACE
+// cells; 2 the face blocks of the boundary kernel, which step only the SFACE
+// cells (kept out of the 40-register bulk kernel, whose registers the
+// reflections would overflow).
+template <int LAT, int EQ, int ST, bool ODD, int MOM, int XF = 0>
 __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int z, int cell, uint8_t flag,
                                           typename Store<ST>::C* diff) {
   using L         = Lattice<LAT>;
@@ -139,8 +181,10 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   T* const      Ac   = static_cast<T*>(P.pop) + cell;  // the cell's slot in plane 0
   const int     NA   = static_cast<int>(P.nalloc);
   bool          work;
-  const bool    xf = ODD && XF && (flag & XFACE);
-  if constexpr(ODD) work = flag == LBM_CELL_FLUID || xf;  // fluid and not LINKED, or stepped in line
+  const bool    xf = ODD && XF == 1 && (flag & XFACE);
+  const bool    sf = ODD && XF == 2 && (flag & SFACE);
+  if constexpr(ODD && XF == 2) work = sf;
+  else if constexpr(ODD) work = flag == LBM_CELL_FLUID || xf;  // fluid and not LINKED, or stepped in line
   else work = type != LBM_CELL_SOLID;
   // the population loads do not wait for the flag: every address stays inside
   // the allocation (guard plane in front, ghost plane behind)
@@ -162,11 +206,15 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   prefetch_moments<C, MOM, NV>(P, cell, prev);
   if(!work) return;
   if constexpr(ODD) {
-    if constexpr(XF) {
+    if constexpr(XF == 1) {
       if(__any_sync(__activemask(), xf)) {
         bulk_finish<LAT, EQ, ST, true, MOM, false, true>(P, y, z, cell, type, f, prev, diff, xf, x);
         return;
       }
+    }
+    if constexpr(XF == 2) {
+      bulk_finish<LAT, EQ, ST, true, MOM, false, true>(P, y, z, cell, type, f, prev, diff, false, x, sf);
+      return;
     }
     bulk_finish<LAT, EQ, ST, true, MOM, false>(P, y, z, cell, type, f, prev, diff);
   } else {
@@ -191,7 +239,7 @@ __device__ __forceinline__ void bulk_grid_cell(const BoxParams& P) {
   for(int k = 0; k < NV; ++k) diff[k] = C(0);
   if(x < P.nx) {
     const int cell = x + P.nx * (y + P.ny * z);
-    bulk_cell<LAT, EQ, ST, ODD, MOM, true>(P, x, y, z, cell, P.flags[cell], diff);
+    bulk_cell<LAT, EQ, ST, ODD, MOM, 1>(P, x, y, z, cell, P.flags[cell], diff);
   }
   if constexpr(MOM == 2) {
     const int64_t b = blockIdx.x + static_cast<int64_t>(gridDim.x) * (blockIdx.y + static_cast<int64_t>(gridDim.y) * blockIdx.z);
@@ -351,9 +399,40 @@ __global__ void k_box_build_links(BoxParams P, const int32_t* list, int n, int32
   });
 }
 
+// The free-slip face cells that the boundary kernel steps without link tables
+// (SFACE cells, per-thread odd step only): positions off the x faces on the
+// two y faces (ny_part of them; for a 2D lattice every slice z) and then on
+// the two z faces, x fastest.  Blocks from list_blocks on take one position
+// per thread; positions without the SFACE bit do nothing.
+struct FaceRange {
+  int64_t ny_part     = 0;
+  int64_t n           = 0;
+  int     list_blocks = 0;
+};
+
+template <int LAT>
+__device__ __forceinline__ void face_position(const BoxParams& P, const FaceRange& fr, int64_t j, int& x, int& y, int& z) {
+  const int64_t w = P.nx - 2;
+  if(j < fr.ny_part) {
+    const int64_t per  = fr.ny_part / 2;
+    const bool    high = j >= per;
+    const int64_t r    = high ? j - per : j;
+    x                  = 1 + static_cast<int>(r % w);
+    z                  = (Lattice<LAT>::D > 2 ? 1 : 0) + static_cast<int>(r / w);
+    y                  = high ? P.ny - 1 : 0;
+  } else {
+    const int64_t per  = (fr.n - fr.ny_part) / 2;
+    const bool    high = j - fr.ny_part >= per;
+    const int64_t r    = high ? j - fr.ny_part - per : j - fr.ny_part;
+    x                  = 1 + static_cast<int>(r % w);
+    y                  = 1 + static_cast<int>(r / w);
+    z                  = high ? P.nz - 1 : 0;
+  }
+}
+
 template <int LAT, int EQ, int ST, int MOM>
 __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* list, int count, int n, int64_t slot0, const int32_t* src,
-                                                 const int32_t* dst, const double* corr_src, const double* corr_dst) {
+                                                 const int32_t* dst, const double* corr_src, const double* corr_dst, FaceRange fr) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -364,7 +443,15 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
   C             diff[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) diff[k] = C(0);
-  if(i < count) {  // the first `count` entries; tables have stride n
+  if(static_cast<int>(blockIdx.x) >= fr.list_blocks) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x - fr.list_blocks) * blockDim.x + threadIdx.x;
+    if(j < fr.n) {
+      int x, y, z;
+      face_position<LAT>(P, fr, j, x, y, z);
+      const int cell = x + P.nx * (y + P.ny * z);
+      bulk_cell<LAT, EQ, ST, true, MOM, 2>(P, x, y, z, cell, P.flags[cell], diff);
+    }
+  } else if(i < count) {  // the first `count` entries; tables have stride n
     const int     cell = list[i];
     const uint8_t type = P.flags[cell] & TYPE_MASK;
     T*            A    = static_cast<T*>(P.pop);
@@ -684,8 +771,16 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   const bool     paired = kind == LBM_BOX_KERNEL_PAIRED && mom == 0;  // residual steps use the per-thread kernel
   // the per-thread odd kernel steps the XFACE cells itself; with the others the
   // boundary kernel takes them too (they close its list)
-  const int      nlist  = static_cast<int>(staged || paired ? b->n_bnd : b->n_bnd_lean);
-  const unsigned nbb    = static_cast<unsigned>((nlist + 127) / 128);
+  // and its SFACE cells are taken by the boundary kernel's face blocks
+  const bool     lean   = !(staged || paired);
+  const int      nlist  = static_cast<int>(lean ? b->n_bnd_lean : b->n_bnd);
+  FaceRange      fr;
+  fr.list_blocks        = (nlist + 127) / 128;
+  if(lean && b->n_sface > 0) {
+    fr.ny_part = b->face_ny_part;
+    fr.n       = b->face_n;
+  }
+  const unsigned nbb    = static_cast<unsigned>(fr.list_blocks + (fr.n + 127) / 128);
   const dim3     gp(static_cast<unsigned>((b->p.nx / 2 + tpb - 1) / tpb), static_cast<unsigned>(b->p.ny), static_cast<unsigned>(b->p.nz));
   if(staged) {
     const cudaError_t e = box_tma_bulk(b, odd, mom, s, &nbulk);
@@ -702,9 +797,9 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     else if(mom == 1) k_box_bulk<LAT, EQ, ST, true, 1><<<g, tpb, 0, s>>>(b->p);
     else k_box_bulk<LAT, EQ, ST, true, 2><<<g, tpb, 0, s>>>(b->p);
     if(nbb) {
-      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
-      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
-      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst);
+      if(mom == 0) k_box_bnd<LAT, EQ, ST, 0><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst, fr);
+      else if(mom == 1) k_box_bnd<LAT, EQ, ST, 1><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst, fr);
+      else k_box_bnd<LAT, EQ, ST, 2><<<nbb, 128, 0, s>>>(b->p, b->bnd_list, nlist, static_cast<int>(b->n_bnd), nbulk, b->link_src, b->link_dst, b->corr_src, b->corr_dst, fr);
     }
     if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
@@ -1198,10 +1293,29 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
         hflags[i] = static_cast<uint8_t>(hflags[i] | XFACE);
         continue;
       }
+      // a fluid cell on exactly one free-slip y / z face, off the x faces:
+      // every link source and destination it reflects to is a non-solid cell
+      // of the box (the cell has no solid stencil neighbour)
+      const bool on_y  = D > 1 && ny >= 3 && (y == 0 || y == ny - 1);
+      const bool on_z  = D > 2 && nz >= 3 && (z == 0 || z == nz - 1);
+      const bool yz_ok = D > 2 ? (y > 0 && y < ny - 1) || (z > 0 && z < nz - 1) : true;
+      const int  sface = on_y && !on_z ? (y == 0 ? 2 : 3) : (on_z && !on_y ? (z == 0 ? 4 : 5) : -1);
+      if(!near && hflags[i] == LBM_CELL_FLUID && nx >= 3 && x > 0 && x < nx - 1 && yz_ok && sface >= 0 &&
+         desc->face[sface] == LBM_FACE_FREESLIP) {
+        xlist.push_back(static_cast<int32_t>(i));
+        hflags[i] = static_cast<uint8_t>(hflags[i] | SFACE);
+        ++b->n_sface;
+        continue;
+      }
       if(near || !inside || hflags[i] != LBM_CELL_FLUID) list.push_back(static_cast<int32_t>(i));
       if(near || !inside) hflags[i] = static_cast<uint8_t>(hflags[i] | LINKED);
     }
     b->n_bnd_lean = static_cast<int64_t>(list.size());
+    // face positions the face blocks walk: every SFACE cell lies among them
+    if(nx >= 3 && ny >= 3 && (D < 3 || nz >= 3) && D > 1) {
+      b->face_ny_part = 2 * static_cast<int64_t>(nx - 2) * (D > 2 ? nz - 2 : nz);
+      b->face_n       = b->face_ny_part + (D > 2 ? 2 * static_cast<int64_t>(nx - 2) * (ny - 2) : 0);
+    }
     list.insert(list.end(), xlist.begin(), xlist.end());
     b->n_bnd = static_cast<int64_t>(list.size());
     if(e == cudaSuccess) e = cudaMalloc(&b->bnd_list, sizeof(int32_t) * std::max<size_t>(1, list.size()));
@@ -1221,7 +1335,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   // residual slots: one per warp of the largest launch over the tuner's block sizes
   int64_t maxrow = 0;
   for(int t : kTunerBlocks) maxrow = std::max<int64_t>(maxrow, static_cast<int64_t>((desc->nx + t - 1) / t) * (t / 32));
-  const int64_t maxblocks = maxrow * desc->ny * desc->nz + static_cast<int64_t>((b->n_bnd + 127) / 128) * 4;
+  const int64_t maxblocks = maxrow * desc->ny * desc->nz + static_cast<int64_t>((b->n_bnd + 127) / 128 + (b->face_n + 127) / 128) * 4;
   if(e == cudaSuccess) e = cudaMalloc(&b->partials, sizeof(double) * (maxblocks * 4 + 304 * 4 + kMidBlocks * 4));
   b->partials_mm      = b->partials + maxblocks * 4;
   b->partials_mid     = b->partials_mm + 304 * 4;

@@ -68,7 +68,10 @@ struct BoxState {
   int          tuned_tpb = 128;
   int32_t*     bnd_list  = nullptr;  // cells the odd step resolves link by link; XFACE cells last
   int64_t      n_bnd     = 0;
-  int64_t      n_bnd_lean = 0;       // leading entries without the XFACE cells (per-thread odd kernel)
+  int64_t      n_bnd_lean = 0;       // leading entries without the XFACE / SFACE cells (per-thread odd kernel)
+  int64_t      n_sface    = 0;       // SFACE cells (free-slip face cells the face blocks step)
+  int64_t      face_ny_part = 0;     // face positions on the y faces, then
+  int64_t      face_n       = 0;     // all face positions (y faces, then z faces)
   int32_t*     link_src  = nullptr;  // n_bnd x Q pull slots of the boundary cells
   int32_t*     link_dst  = nullptr;  // n_bnd x Q push slots (-1: leaves the box)
   double*      corr_src  = nullptr;  // moving-wall terms (allocated only when a wall moves)

@@ -22,7 +22,25 @@ constexpr uint8_t XFACE      = 0x10;  // set by the engine: an inlet cell on an 
                                      // per-thread odd step handles it in line (emit, or ghost pulls, and
                                      // no push through the face), the other bulk kernels leave it to the
                                      // boundary kernel
+constexpr uint8_t SFACE      = 0x20;  // set by the engine: a fluid cell on exactly one free-slip y or z face,
+                                     // away from solids and the x faces; the per-thread odd step pulls
+                                     // and pushes its links through that face by specular reflection in
+                                     // line, the other bulk kernels leave it to the boundary kernel
 // ---- link resolution ---------------------------------------------------------
+// direction q with its component along axis AX reversed (compile-time form of
+// mirror() for one axis)
+template <int LAT, int AX>
+LBM_HD constexpr int mirror_axis(int q) {
+  using L = Lattice<LAT>;
+  for(int k = 0; k < L::Q; ++k) {
+    bool same = true;
+    for(int a = 0; a < 3; ++a)
+      if(L::c(k, a) != (a == AX ? -L::c(q, a) : L::c(q, a))) same = false;
+    if(same) return k;
+  }
+  return q;
+}
+
 // mirror of direction q in the axes of `mask` (free-slip reflection)
 template <int LAT>
 __device__ __forceinline__ int mirror(int q, int mask) {

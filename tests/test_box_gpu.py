@@ -61,6 +61,15 @@ CASES = {
     "d2q9_cavity": dict(lattice=2, shape=(12, 12, 1), omega=1 / 0.6, faces=("wall",) * 6, lid=(3, (0.1, 0.0, 0.0))),
     "d2q9_open_cylinder": dict(lattice=2, shape=(30, 12, 1), omega=1 / 0.6, faces=("open", "open", "freeslip", "wall", "wall", "wall"),
                                sphere=((9.0, 6.0, 0.5), 2.6), inlet=(0.04, 0, 0)),
+    # free-slip cells on both y faces of three stacked 2D slices, with a body
+    # force along x (the per-thread step reflects them without link tables)
+    "d2q9_slices_freeslip": dict(lattice=2, shape=(20, 9, 3), omega=1 / 0.7,
+                                 faces=("periodic", "periodic", "freeslip", "freeslip", "wall", "wall"), force=(1e-5, 2e-6, 0)),
+    # free slip on all four side faces, a sphere touching none of them, and a
+    # force with components along every axis
+    "d3q19_freeslip_box": dict(lattice=4, shape=(16, 11, 9), omega=1 / 0.62,
+                               faces=("periodic", "periodic", "freeslip", "freeslip", "freeslip", "freeslip"),
+                               sphere=((8.0, 5.5, 4.5), 2.2), force=(1e-5, 3e-6, -2e-6)),
     # rows longer than one staged segment (256 cells), the last one partial
     "d3q19_long_rows": dict(lattice=4, shape=(520, 10, 8), omega=1 / 0.55, faces=("open", "open", "freeslip", "freeslip", "wall", "wall"),
                             sphere=((255.0, 5.0, 4.0), 3.1), inlet=(0.05, 0, 0)),
