@@ -50,18 +50,30 @@ CASES = [
     ("poisson2d_helmholtz_small", ("own", "poisson2d_helmholtz_small.json"), [100]),
     ("cavity_small", ("own", "cavity_small.json"), [1, 100]),
     ("channel_mixed_small", ("own", "channel_mixed_small.json"), [1, 100]),
+    # the reference's 2D flow around an obstacle (box minus a circle, pressure
+    # inlet / outlet, bounce-back walls) at level 5 instead of 8
+    ("sphere_ns_l5", ("ref", "test/sphere/sphere_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}),
+     [1, 60]),
 ]
 
 
 def config_path(src):
-    kind, rel = src
+    kind, rel = src[0], src[1]
     return os.path.join(REF, rel) if kind == "ref" else os.path.join(HERE, "cases", rel)
 
 
-def run_case(name, src, steps):
-    cfg_path = config_path(src)
-    with open(cfg_path) as fh:
+def load_config(src):
+    """The case's JSON config; a third element of ``src`` holds top-level keys
+    that replace the file's (a reference test case at a coarser level)."""
+    with open(config_path(src)) as fh:
         cfg = json.load(fh)
+    if len(src) > 2:
+        cfg.update(src[2])
+    return cfg
+
+
+def run_case(name, src, steps):
+    cfg = load_config(src)
     with tempfile.TemporaryDirectory() as tmp:
         # the harness writes logs into its working directory
         local_cfg = os.path.join(tmp, "case.json")
@@ -89,8 +101,7 @@ VTP_CASES = [("cavity_small", 100), ("poisson2d_helmholtz_small", 100)]
 
 def run_vtp(name, steps):
     src = next(s for n, s, _ in CASES if n == name)
-    with open(config_path(src)) as fh:
-        cfg = json.load(fh)
+    cfg = load_config(src)
     with tempfile.TemporaryDirectory() as tmp:
         local_cfg = os.path.join(tmp, "case.json")
         with open(local_cfg, "w") as fh:
@@ -125,8 +136,7 @@ LINE_CASES = [
 
 def run_line(name, steps, tag, a, b):
     src = next(s for n, s, _ in CASES if n == name)
-    with open(config_path(src)) as fh:
-        cfg = json.load(fh)
+    cfg = load_config(src)
     cfg["solver"]["postprocessing"] = {"line1": {"type": "line", "execute": "atEnd", "A": a, "B": b}}
     with tempfile.TemporaryDirectory() as tmp:
         local_cfg = os.path.join(tmp, "case.json")
