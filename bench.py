@@ -42,7 +42,7 @@ METRIC = "MLUPS (D3Q19 sphere 512x256x256, FP16-deviation storage)"
 # DRAM bytes (read + write) per step of this workload, averaged over the two
 # step parities (bulk + boundary + outlet kernels), from the one-pass ncu
 # launch list recorded in profiles/launches_bench_d3q19_sphere_512x256x256.md
-MEASURED_TRAFFIC_PER_STEP = {"f16dev": 2.71e9}
+MEASURED_TRAFFIC_PER_STEP = {"f16dev": 2.58e9}
 
 
 def peaks():
