@@ -1,0 +1,107 @@
+/* Host-side grid and table build for the GB300 LBM library (C ABI).
+ *
+ * Builds, from an analytic geometry (boxes and spheres, bodies with
+ * subtracted objects), the uniform Cartesian grid that the SFCMM/LBM
+ * reference's grid generator and CartesianGrid produce when
+ * partitionLevel == uniformLevel == maxRfnmtLvl (every reference LBM case),
+ * and the tables its LBM solver reads:
+ *
+ *   entry point                  reference step it replaces
+ *   lbm_grid_create              GridGenerator::init / createPartitioningGrid, deleteOutsideCells,
+ *                                reorderHilbertCurve (src/gridgenerator/gridGenerator.cpp:255-287,
+ *                                src/gridgenerator/cartesiangrid_generation.h:71-149, 505-610, 664-735),
+ *                                GeometryManager (src/geometry.h:923-1104), bounding box and level
+ *                                lengths (src/cartesiangrid_base.h:125-142)
+ *   lbm_grid_align               GridGenerator's alignNodesWithSurface step
+ *                                (src/gridgenerator/cartesiangrid_generation.h:255-300)
+ *   lbm_grid_boundary            CartesianGrid::determineBoundaryCells (src/cartesiangrid.h:509-544)
+ *   lbm_grid_add_surface         CartesianGrid::identifyBndrySurfaces, one surface entry
+ *                                (src/cartesiangrid.h:551-598)
+ *   lbm_grid_connect_periodic    CartesianGrid::addPeriodicConnection (src/cartesiangrid.h:636-703)
+ *   lbm_grid_neighbors           the neighbour table after addDiagonalNghbrs (src/cartesiangrid.h:450-487)
+ *
+ * In 2D (and 1D) every table equals the reference's bit for bit.  In 3D,
+ * where the reference stops (box and sphere cut tests, src/geometry.h:690-692
+ * and 796-798; diagonal neighbours, src/cartesiangrid.h:483-485), the same
+ * rules are extended to the third dimension: a box cell is cut when it
+ * touches one of the six faces within the face's extent, a sphere cell when
+ * the sphere surface passes between its eight vertices, and the twelve
+ * edge neighbours are formed through the main neighbours (x step first,
+ * then y, then z), indexed in the D3Q19 direction order.
+ *
+ * All calls are host-only (no device memory, no CUDA call).  Status codes
+ * are those of lbm_gpu.h.
+ */
+#ifndef LBM_GRID_H
+#define LBM_GRID_H
+
+#include <stdint.h>
+
+#include "lbm_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_GEOM_BOX 0
+#define LBM_GEOM_SPHERE 1
+
+typedef struct lbm_geom_desc {
+  int32_t kind;      /* LBM_GEOM_BOX or LBM_GEOM_SPHERE */
+  int32_t body;      /* objects with the same body id form one body ("body" key) */
+  int32_t subtract;  /* 1: the object is removed from its body ("subtract" key) */
+  int32_t reserved;
+  double  a[3];      /* box corner A */
+  double  b[3];      /* box corner B */
+  double  center[3]; /* sphere centre */
+  double  radius;    /* sphere radius */
+} lbm_geom_desc;
+
+typedef struct lbm_grid lbm_grid;
+
+/* The grid at `level` over `bbox` (2*ndim values min0,max0,min1,...; NULL:
+ * the union of the objects' bounding boxes): the cells cut by an object or
+ * with their centre inside the geometry, in the curve order of
+ * hilbert::index (include/common/math/hilbert.h:16-48), with their main
+ * neighbours.  Objects are given in the order of the config's "geometry"
+ * keys (sorted). */
+int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int32_t nobj, const double* bbox, lbm_grid** out);
+
+/* "alignNodesWithSurface": stretch the grid so that the outermost cell
+ * centres along `align_dir` (along every axis when the centres span the same
+ * range on all of them) lie on the bounding box, scale the cell length with
+ * it, and delete the cells that are then neither cut nor inside, as the
+ * reference's GridGenerator does (transformMaxRfnmtLvlToExtent,
+ * src/gridgenerator/cartesiangrid_generation.h:255-300).  Call before any
+ * surface. */
+int lbm_grid_align(lbm_grid* g, int32_t align_dir);
+
+int64_t lbm_grid_ncells(const lbm_grid* g);
+/* width of the neighbour table: 2 (1D), 8 (2D), 18 (3D) */
+int32_t lbm_grid_nnghbr(const lbm_grid* g);
+/* bounding box (2*ndim) and the cell length of the grid level */
+int lbm_grid_info(const lbm_grid* g, double* bbox, double* cell_length);
+/* cell centres, ncells x ndim, curve order */
+int lbm_grid_centers(const lbm_grid* g, double* out);
+/* boundary property per cell: cut by the geometry and missing a main neighbour */
+int lbm_grid_boundary(const lbm_grid* g, uint8_t* out);
+/* One surface of a "boundary" entry: for each direction in [dir_begin,
+ * dir_end) and each boundary cell without a main neighbour in it that
+ * object `obj` cuts, the pair (cell, direction) unless an earlier call took
+ * it.  Appends up to `cap` pairs to cells / dirs, in the reference's order;
+ * *n = number of pairs (LBM_ERR_INVALID if more than cap). */
+int lbm_grid_add_surface(lbm_grid* g, int32_t obj, int32_t dir_begin, int32_t dir_end, int64_t* cells, int8_t* dirs, int64_t cap,
+                         int64_t* n);
+/* Connect the cells of two periodic surfaces whose centres differ along
+ * exactly one axis (main neighbours across the period). */
+int lbm_grid_connect_periodic(lbm_grid* g, const int64_t* cells_a, int64_t na, const int64_t* cells_b, int64_t nb);
+/* neighbour table, ncells x nnghbr (-1: none): main directions, then the
+ * diagonals built from them */
+int lbm_grid_neighbors(const lbm_grid* g, int64_t* out);
+void lbm_grid_destroy(lbm_grid* g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GRID_H */

@@ -1,0 +1,200 @@
+"""Grid tables from the reference's JSON config, without its grid generator.
+
+The SFCMM/LBM reference builds the LBM grid in two programs: the grid
+generator (``src/gridgenerator/``) makes the cells, and ``CartesianGrid::
+loadGridInplace`` (src/cartesiangrid.h:264-320) derives the boundary cells,
+the named boundary surfaces, the periodic wiring and the diagonal neighbours.
+:func:`grid_tables` does both for the uniform grids every reference LBM case
+uses (``partitionLevel == uniformLevel == maxRfnmtLvl``) and returns the
+:class:`~lbm_gb300.refconfig.GridTables` the solvers consume.  The per-cell
+work runs in the native library (include/lbm_grid.h); this module walks the
+config in the reference's order:
+
+1. geometry objects in sorted key order (nlohmann::json iterates sorted),
+   each with its body (``"body"``, default its own name) and ``"subtract"``;
+2. the grid at the uniform level (``lbm_grid_create``), stretched onto the
+   geometry's surface when ``"alignNodesWithSurface"`` is set
+   (``lbm_grid_align``, along ``"alignDir"``, default 1);
+3. surfaces (identifyBndrySurfaces, src/cartesiangrid.h:551-598): for each
+   geometry of ``solver.boundary`` and each of its direction entries, both in
+   sorted order, the surface ``<geometry>_<dir>`` (or ``<geometry>`` when it
+   has one entry) takes the boundary cells without a neighbour in that
+   direction that the geometry cuts, unless an earlier surface took the
+   (cell, direction) pair.  A cell keeps the normal of the last direction it
+   was added with (``Surface::addCell`` stores normals per cell,
+   src/common/surface.h:52-55);
+4. periodic surfaces with ``"generateBndry": false`` are wired across the
+   period (setupPeriodicConnections, src/cartesiangrid.h:600-634);
+5. the diagonal neighbours (addDiagonalNghbrs, src/cartesiangrid.h:450-487).
+
+In 2D and 1D the tables equal the reference's bit for bit; 3D, which the
+reference cannot build, follows the same rules (include/lbm_grid.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, List
+
+import numpy as np
+
+from . import _lib
+from .refconfig import ConfigError, GridTables
+
+GEOM_BOX = 0
+GEOM_SPHERE = 1
+DIRS = {"-x": 0, "+x": 1, "-y": 2, "+y": 3, "-z": 4, "+z": 5}
+
+
+class GeomDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("body", C.c_int32), ("subtract", C.c_int32), ("reserved", C.c_int32),
+                ("a", C.c_double * 3), ("b", C.c_double * 3), ("center", C.c_double * 3), ("radius", C.c_double)]
+
+
+_SIGS = {
+    "lbm_grid_create": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "lbm_grid_align": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lbm_grid_ncells": (C.c_int64, [C.c_void_p]),
+    "lbm_grid_nnghbr": (C.c_int32, [C.c_void_p]),
+    "lbm_grid_info": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "lbm_grid_centers": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_grid_boundary": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_grid_add_surface": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int64,
+                                       C.POINTER(C.c_int64)]),
+    "lbm_grid_connect_periodic": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]),
+    "lbm_grid_neighbors": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_grid_destroy": (None, [C.c_void_p]),
+}
+
+
+def _grid_lib():
+    lib = _lib.load()
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def _vec(values, ndim: int, what: str) -> List[float]:
+    v = [float(x) for x in values]
+    if len(v) != ndim:
+        raise ConfigError(f"{what}: expected {ndim} values, got {len(v)}")
+    return v + [0.0] * (3 - ndim)
+
+
+def geometry_objects(geometry: Dict, ndim: int):
+    """GeomDesc array and names, in the reference's (sorted) order."""
+    names = sorted(geometry)
+    descs = (GeomDesc * max(1, len(names)))()
+    bodies: Dict[str, int] = {}
+    for i, name in enumerate(names):
+        g = geometry[name]
+        if "type" not in g:
+            raise ConfigError(f'geometry "{name}": no "type" given')
+        d = descs[i]
+        if g["type"] == "box":
+            d.kind = GEOM_BOX
+            d.a[:] = _vec(g["A"], ndim, f"{name}.A")
+            d.b[:] = _vec(g["B"], ndim, f"{name}.B")
+        elif g["type"] == "sphere":
+            d.kind = GEOM_SPHERE
+            d.center[:] = _vec(g["center"], ndim, f"{name}.center")
+            d.radius = float(g["radius"])
+        else:
+            raise ConfigError(f'geometry "{name}": type "{g["type"]}" is not supported (box, sphere)')
+        body = g.get("body", "unique")
+        body = name if body == "unique" else body
+        d.body = bodies.setdefault(body, len(bodies))
+        d.subtract = 1 if g.get("subtract", False) else 0
+    return descs, names
+
+
+def grid_tables(config: Dict) -> GridTables:
+    """The reference's LBM grid tables for a JSON config (the grid generator's
+    keys plus ``solver.boundary``)."""
+    ndim = int(config.get("dim", 0))
+    if ndim not in (1, 2, 3):
+        raise ConfigError(f"dim must be 1, 2 or 3, got {ndim}")
+    levels = {k: int(config[k]) for k in ("partitionLevel", "uniformLevel", "maxRfnmtLvl") if k in config}
+    level = levels.get("uniformLevel", levels.get("partitionLevel"))
+    if level is None or len(set(levels.values())) != 1:
+        raise ConfigError("only uniform grids are built: partitionLevel, uniformLevel and maxRfnmtLvl must be equal")
+    geometry = config.get("geometry", {})
+    descs, names = geometry_objects(geometry, ndim)
+    bbox = None
+    if not names or "boundingBox" in config:
+        default = [0.0, 1.0] * ndim
+        bbox = (C.c_double * (2 * ndim))(*[float(x) for x in config.get("boundingBox", default)])
+    lib = _grid_lib()
+    h = C.c_void_p()
+    rc = lib.lbm_grid_create(ndim, level, C.cast(descs, C.c_void_p), len(names), C.cast(bbox, C.c_void_p) if bbox else None,
+                             C.byref(h))
+    _lib.check(rc, what="lbm_grid_create")
+    try:
+        if config.get("alignNodesWithSurface", False):
+            _lib.check(lib.lbm_grid_align(h, int(config.get("alignDir", 1))), what="lbm_grid_align")
+        n = int(lib.lbm_grid_ncells(h))
+        centers = np.empty((n, ndim), dtype=np.float64)
+        _lib.check(lib.lbm_grid_centers(h, centers.ctypes.data), what="lbm_grid_centers")
+        box = np.empty(2 * ndim, dtype=np.float64)
+        cl = C.c_double()
+        _lib.check(lib.lbm_grid_info(h, box.ctypes.data, C.byref(cl)), what="lbm_grid_info")
+
+        surfaces: Dict[str, dict] = {}
+        periodic = {}
+        boundary = config.get("solver", {}).get("boundary", {})
+        cap = n * 2 * ndim
+        cells = np.empty(cap, dtype=np.int64)
+        dirs = np.empty(cap, dtype=np.int8)
+        for gname in sorted(boundary):
+            entries = boundary[gname]
+            for dname in sorted(entries):
+                sname = f"{gname}_{dname}" if len(entries) > 1 else gname
+                if dname == "all":
+                    d0, d1 = 0, 2 * ndim
+                elif dname in DIRS and DIRS[dname] < 2 * ndim:
+                    d0 = DIRS[dname]
+                    d1 = d0 + 1
+                else:
+                    raise ConfigError(f'boundary "{gname}": invalid direction "{dname}"')
+                got = C.c_int64()
+                if gname in names:
+                    _lib.check(lib.lbm_grid_add_surface(h, names.index(gname), d0, d1, cells.ctypes.data, dirs.ctypes.data, cap,
+                                                        C.byref(got)), what="lbm_grid_add_surface")
+                m = int(got.value)
+                lst = cells[:m].copy()
+                last = {}
+                for c, d in zip(lst.tolist(), dirs[:m].tolist()):
+                    last[c] = d  # Surface::addCell keeps one normal per cell: the last
+                normals = np.zeros((m, ndim), dtype=np.float64)
+                for i, c in enumerate(lst.tolist()):
+                    d = last[c]
+                    normals[i, d // 2] = 1.0 if d & 1 else -1.0
+                surfaces[sname] = {"cells": lst, "normals": normals}
+                e = entries[dname]
+                if isinstance(e, dict) and e.get("type") == "periodic" and not e.get("generateBndry", True):
+                    if "connection" not in e:
+                        raise ConfigError(f'periodic boundary "{gname}_{dname}" without "connection"')
+                    periodic[f"{gname}_{dname}"] = e["connection"]
+        # wire each connected pair once (the pairing is symmetric)
+        done = set()
+        for a in sorted(periodic):
+            b = periodic[a]
+            if a in done:
+                continue
+            if periodic.get(b) is None:
+                raise ConfigError("Invalid periodic setup!")
+            done.update((a, b))
+            for s in (a, b):
+                if s not in surfaces:
+                    raise ConfigError(f'periodic connection to unknown surface "{s}"')
+            ca, cb = surfaces[a]["cells"], surfaces[b]["cells"]
+            _lib.check(lib.lbm_grid_connect_periodic(h, ca.ctypes.data, len(ca), cb.ctypes.data, len(cb)),
+                       what="lbm_grid_connect_periodic")
+        w = int(lib.lbm_grid_nnghbr(h))
+        nghbr = np.empty((n, w), dtype=np.int64)
+        _lib.check(lib.lbm_grid_neighbors(h, nghbr.ctypes.data), what="lbm_grid_neighbors")
+    finally:
+        lib.lbm_grid_destroy(h)
+    return GridTables(ndim=ndim, centers=centers, nghbr=nghbr, surfaces=surfaces, bbox=box, cell_length=float(cl.value),
+                      max_lvl=level)

@@ -154,10 +154,31 @@ def run_line(name, steps, tag, a, b):
     print(f"{os.path.basename(dst)}: {data.count(b'\n') - 1} points")
 
 
+# the grid part of every case's config (grid generator keys, geometry and the
+# solver's boundary block): tests/golden/grid_configs.json, the input of the
+# grid-table tests (the reference's own test configs are not read at test time)
+GRID_KEYS = ("dim", "partitionLevel", "uniformLevel", "maxRfnmtLvl", "boundingBox", "alignNodesWithSurface", "alignDir", "geometry")
+
+
+def write_grid_configs():
+    out = {}
+    for name, src, _ in CASES:
+        cfg = load_config(src)
+        g = {k: cfg[k] for k in GRID_KEYS if k in cfg}
+        g["solver"] = {"boundary": cfg["solver"]["boundary"]}
+        out[name] = g
+    with open(os.path.join(HERE, "grid_configs.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+        fh.write("\n")
+    print(f"grid_configs.json: {len(out)} cases")
+
+
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
     wanted = set(argv[1:])
+    if not wanted or "grid_configs" in wanted:
+        write_grid_configs()
     for name, src, steps in CASES:
         if wanted and name not in wanted:
             continue

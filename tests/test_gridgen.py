@@ -1,0 +1,137 @@
+"""The native grid and table build against the reference's own grids.
+
+Every golden fixture holds the grid tables the reference's LBMSolver saw: the
+cell centres in curve order, the neighbour table after the periodic wiring and
+the diagonal neighbours, and the named boundary surfaces with their normals.
+lbm_gb300.gridgen builds them from the case's JSON config alone
+(tests/golden/grid_configs.json, written by make_golden.py from the same
+configs); they must be equal bit for bit.  The library call is host-only, so
+these tests run without a GPU.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import caseio
+from lbm_gb300 import gridgen
+from lbm_gb300.refconfig import ConfigError
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CONFIGS = json.load(open(os.path.join(HERE, "golden", "grid_configs.json")))
+FIXTURES = caseio.list_fixtures()
+
+
+def case_of(fixture):
+    return fixture.rsplit("_", 1)[0]
+
+
+def test_every_fixture_has_its_grid_config():
+    assert {case_of(f) for f in FIXTURES} <= set(CONFIGS)
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_grid_tables_equal_the_reference(name):
+    _, _, ref, _ = caseio.load(name)
+    g = gridgen.grid_tables(CONFIGS[case_of(name)])
+    assert g.ndim == ref.ndim
+    assert np.array_equal(g.centers, ref.centers)
+    assert np.array_equal(g.nghbr, ref.nghbr)
+    assert g.cell_length == ref.cell_length
+    assert np.array_equal(g.bbox, ref.bbox)
+    assert g.max_lvl == ref.max_lvl
+    assert sorted(g.surfaces) == sorted(ref.surfaces)
+    for k, s in ref.surfaces.items():
+        assert np.array_equal(g.surfaces[k]["cells"], s["cells"]), k
+        assert np.array_equal(g.surfaces[k]["normals"], s["normals"]), k
+
+
+def test_obstacle_surface_repeats_cells_with_their_last_normal():
+    """The reference's circle surface lists a cell once per missing direction
+    but keeps one normal per cell (the last)."""
+    g = gridgen.grid_tables(CONFIGS["sphere_ns_l5"])
+    s = g.surfaces["sphere"]
+    cells = s["cells"].tolist()
+    assert len(cells) > len(set(cells))
+    for c in set(cells):
+        rows = s["normals"][[i for i, x in enumerate(cells) if x == c]]
+        assert (rows == rows[0]).all()
+
+
+def _sphere_box_3d(level=5, r=0.2):
+    return {"dim": 3, "partitionLevel": level, "uniformLevel": level, "maxRfnmtLvl": level,
+            "geometry": {"box": {"type": "box", "A": [0.0, 0.0, 0.0], "B": [2.0, 1.0, 1.0], "body": "fluid"},
+                         "ball": {"type": "sphere", "center": [0.6, 0.5, 0.45], "radius": r, "body": "fluid", "subtract": True}},
+            "solver": {"boundary": {"box": {"-x": {"type": "periodic", "generateBndry": False, "connection": "box_+x"},
+                                            "+x": {"type": "periodic", "generateBndry": False, "connection": "box_-x"},
+                                            "-y": {"type": "wall"}, "+y": {"type": "wall"}, "-z": {"type": "wall"},
+                                            "+z": {"type": "wall"}},
+                                    "ball": {"all": {"type": "wall"}}}}}
+
+
+def test_3d_box_with_a_sphere():
+    """3D, which the reference cannot build: the cut layer around the box,
+    the sphere's cells removed, periodic x wiring, symmetric links and edge
+    neighbours consistent with two main steps."""
+    level = 5
+    g = gridgen.grid_tables(_sphere_box_3d(level))
+    h = 2.0 / 2 ** level
+    assert g.cell_length == h
+    assert g.nghbr.shape[1] == 18
+    c = g.centers
+    # the box is [0,2]x[0,1]x[0,1]; along y and z the cut layer keeps one row
+    # of centres half a cell outside each face (the reference's 2D rule, here
+    # on six faces); along x, the longest axis, the root cell spans the box
+    # exactly and the outermost centres lie half a cell inside
+    for d in (1, 2):
+        assert np.isclose(c[:, d].min(), -h / 2) and np.isclose(c[:, d].max(), 1 + h / 2)
+    assert np.isclose(c[:, 0].min(), h / 2) and np.isclose(c[:, 0].max(), 2 - h / 2)
+    # no centre deep inside the ball
+    assert (np.linalg.norm(c - [0.6, 0.5, 0.45], axis=1) > 0.2 - h).all()
+    # every cell is unique and sits on the level's lattice
+    k = np.round((c + h / 2) / h).astype(np.int64)
+    assert len({tuple(x) for x in k.tolist()}) == len(k)
+    # main links are symmetric; the x links wrap
+    n = g.ncells
+    for d in range(6):
+        nb = g.nghbr[:, d]
+        has = nb >= 0
+        assert (g.nghbr[nb[has], d ^ 1] == np.arange(n)[has]).all()
+    east = g.nghbr[:, 1]
+    wrap = (east >= 0) & (c[np.maximum(east, 0), 0] < c[:, 0])
+    assert wrap.sum() > 0 and np.allclose(c[wrap, 0], 2 - h / 2)
+    # edge neighbour (+x,+y) is the +y neighbour of the +x neighbour
+    px = g.nghbr[:, 1]
+    exp = np.where(px >= 0, g.nghbr[np.maximum(px, 0), 3], -1)
+    assert np.array_equal(g.nghbr[:, 6 + 3], exp)
+    # surfaces: walls on y and z, the ball on its own, periodic x faces
+    assert {"box_-y", "box_+y", "box_-z", "box_+z", "box_-x", "box_+x", "ball"} == set(g.surfaces)
+    assert len(g.surfaces["ball"]["cells"]) > 0
+    assert (g.surfaces["box_+z"]["normals"] == [0, 0, 1]).all()
+
+
+def test_curve_order_is_the_reference_u_order():
+    """The first cells of a 2D unit box follow the quadrant order (lo,lo),
+    (lo,hi), (hi,hi), (hi,lo) of the reference's curve
+    (UnitTest/test_hilbert.cpp pins hilbert::index)."""
+    cfg = {"dim": 2, "partitionLevel": 3, "uniformLevel": 3, "maxRfnmtLvl": 3,
+           "geometry": {"cube": {"type": "box", "A": [0.0, 0.0], "B": [1.0, 1.0]}}, "solver": {"boundary": {}}}
+    g = gridgen.grid_tables(cfg)
+    assert g.ncells == 64
+    assert g.centers[:4].tolist() == [[0.0625, 0.0625], [0.0625, 0.1875], [0.1875, 0.1875], [0.1875, 0.0625]]
+
+
+def test_config_errors():
+    base = _sphere_box_3d(4)
+    bad = dict(base, uniformLevel=5)
+    with pytest.raises(ConfigError):
+        gridgen.grid_tables(bad)
+    bad = json.loads(json.dumps(base))
+    bad["geometry"]["box"]["type"] = "stl"
+    with pytest.raises(ConfigError):
+        gridgen.grid_tables(bad)
+    bad = json.loads(json.dumps(base))
+    del bad["solver"]["boundary"]["box"]["+x"]
+    with pytest.raises(ConfigError):
+        gridgen.grid_tables(bad)
