@@ -76,6 +76,11 @@ int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int3
  * surface. */
 int lbm_grid_align(lbm_grid* g, int32_t align_dir);
 
+/* hilbert::index of a point x (ndim values in the unit cube, ndim <= 4) at
+ * `level` (include/common/math/hilbert.h:16-48): the key the cells are
+ * sorted by */
+int lbm_grid_curve_index(int32_t ndim, int32_t level, const double* x, uint64_t* out);
+
 int64_t lbm_grid_ncells(const lbm_grid* g);
 /* width of the neighbour table: 2 (1D), 8 (2D), 18 (3D) */
 int32_t lbm_grid_nnghbr(const lbm_grid* g);

@@ -143,7 +143,7 @@ bool geom_cut(const lbm_grid& g, const double* c, double len) {
 // unit cube
 uint64_t curve_index(const double* x, int D, int level) {
   static constexpr int lut[16] = {0, 3, 1, 2, 5, 4, 6, 7, 10, 9, 11, 8, 15, 14, 12, 13};
-  double               p[3];
+  double               p[4];
   for(int d = 0; d < D; ++d) p[d] = x[d];
   uint64_t index = 0;
   for(int l = 0; l < level; ++l) {
@@ -383,6 +383,12 @@ int lbm_grid_align(lbm_grid* g, int32_t align_dir) {
   g->centers.resize(end * D);
   g->ipos.resize(end * D);
   link_cells(*g);
+  return LBM_OK;
+}
+
+int lbm_grid_curve_index(int32_t ndim, int32_t level, const double* x, uint64_t* out) {
+  if(ndim < 1 || ndim > 4 || level < 0 || static_cast<int64_t>(ndim) * level > 64 || !x || !out) return LBM_ERR_INVALID;
+  *out = curve_index(x, ndim, level);
   return LBM_OK;
 }
 

@@ -53,6 +53,7 @@ class GeomDesc(C.Structure):
 _SIGS = {
     "lbm_grid_create": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "lbm_grid_align": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lbm_grid_curve_index": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_uint64)]),
     "lbm_grid_ncells": (C.c_int64, [C.c_void_p]),
     "lbm_grid_nnghbr": (C.c_int32, [C.c_void_p]),
     "lbm_grid_info": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
@@ -80,6 +81,14 @@ def _vec(values, ndim: int, what: str) -> List[float]:
     if len(v) != ndim:
         raise ConfigError(f"{what}: expected {ndim} values, got {len(v)}")
     return v + [0.0] * (3 - ndim)
+
+
+def curve_index(x, level: int) -> int:
+    """The reference's curve index (hilbert::index) of a point in the unit cube."""
+    p = np.ascontiguousarray(x, dtype=np.float64)
+    out = C.c_uint64()
+    _lib.check(_grid_lib().lbm_grid_curve_index(len(p), level, p.ctypes.data, C.byref(out)), what="lbm_grid_curve_index")
+    return int(out.value)
 
 
 def geometry_objects(geometry: Dict, ndim: int):

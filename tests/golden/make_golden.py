@@ -173,12 +173,35 @@ def write_grid_configs():
     print(f"grid_configs.json: {len(out)} cases")
 
 
+# known answers of the reference's curve index (UnitTest/test_hilbert.cpp):
+# every EXPECT_EQ(hilbert::index<N>(point, level), value) with its point ->
+# tests/golden/hilbert_kat.json
+def write_hilbert_kat():
+    import re
+    src = open(os.path.join(REF, "UnitTest", "test_hilbert.cpp")).read()
+    points, kat = {}, []
+    for line in src.splitlines():
+        m = re.match(r"\s*VectorD<(\d)>\s+(\w+)\s*=\s*\{([^}]*)\};", line)
+        if m:
+            points[m.group(2)] = [float(v) for v in m.group(3).split(",")]
+            continue
+        m = re.match(r"\s*EXPECT_EQ\(hilbert::index<(\d)>\((\w+),\s*(\d+)\),\s*(\d+)\);", line)
+        if m:
+            kat.append({"ndim": int(m.group(1)), "x": points[m.group(2)], "level": int(m.group(3)), "index": int(m.group(4))})
+    with open(os.path.join(HERE, "hilbert_kat.json"), "w") as fh:
+        json.dump(kat, fh, indent=0)
+        fh.write("\n")
+    print(f"hilbert_kat.json: {len(kat)} known answers")
+
+
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
     wanted = set(argv[1:])
     if not wanted or "grid_configs" in wanted:
         write_grid_configs()
+    if not wanted or "hilbert_kat" in wanted:
+        write_hilbert_kat()
     for name, src, steps in CASES:
         if wanted and name not in wanted:
             continue

@@ -111,6 +111,17 @@ def test_3d_box_with_a_sphere():
     assert (g.surfaces["box_+z"]["normals"] == [0, 0, 1]).all()
 
 
+KAT = json.load(open(os.path.join(HERE, "golden", "hilbert_kat.json")))
+
+
+def test_curve_index_known_answers():
+    """Every known answer of the reference's own curve-index tests
+    (UnitTest/test_hilbert.cpp, 2D to 4D)."""
+    assert len(KAT) == 125
+    for k in KAT:
+        assert gridgen.curve_index(k["x"], k["level"]) == k["index"], k
+
+
 def test_curve_order_is_the_reference_u_order():
     """The first cells of a 2D unit box follow the quadrant order (lo,lo),
     (lo,hi), (hi,hi), (hi,lo) of the reference's curve
