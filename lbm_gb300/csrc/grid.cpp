@@ -46,6 +46,7 @@ struct lbm_grid {
   std::vector<int32_t>       ipos;       // n x D integer positions on the level
   std::vector<int64_t>       nbr;        // n x 2D main neighbours
   std::vector<uint8_t>       bndry;      // boundary property
+  std::vector<int64_t>       bcells;     // the boundary cells, ascending
   std::vector<uint8_t>       assigned;   // per cell: bit d set when (cell, d) belongs to a surface
 };
 
@@ -186,6 +187,9 @@ void link_cells(lbm_grid& g) {
     for(int dir = 0; dir < M; ++dir) present += g.nbr[c * M + dir] != -1;
     g.bndry[c] = present < M;
   }
+  g.bcells.clear();
+  for(int64_t c = 0; c < g.n; ++c)
+    if(g.bndry[c]) g.bcells.push_back(c);
 }
 
 }  // namespace
@@ -429,8 +433,8 @@ int lbm_grid_add_surface(lbm_grid* g, int32_t obj, int32_t dir_begin, int32_t di
   if(dir_begin < 0 || dir_end > M || dir_begin >= dir_end) return LBM_ERR_INVALID;
   int64_t count = 0;
   for(int dir = dir_begin; dir < dir_end; ++dir)
-    for(int64_t c = 0; c < g->n; ++c) {
-      if(!g->bndry[c] || g->nbr[c * M + dir] != -1) continue;
+    for(const int64_t c : g->bcells) {  // the boundary cells in cell order
+      if(g->nbr[c * M + dir] != -1) continue;
       if(!obj_cut(g->objs[obj], &g->centers[c * D], g->cell_length, D)) continue;
       if(g->assigned[c] & (1u << dir)) continue;  // taken by an earlier surface
       g->assigned[c] = static_cast<uint8_t>(g->assigned[c] | (1u << dir));

@@ -172,13 +172,11 @@ def grid_tables(config: Dict) -> GridTables:
                                                         C.byref(got)), what="lbm_grid_add_surface")
                 m = int(got.value)
                 lst = cells[:m].copy()
-                last = {}
-                for c, d in zip(lst.tolist(), dirs[:m].tolist()):
-                    last[c] = d  # Surface::addCell keeps one normal per cell: the last
+                # Surface::addCell keeps one normal per cell: that of its last entry
+                last = {c: d for c, d in zip(lst.tolist(), dirs[:m].tolist())}
+                dl = np.array([last[c] for c in lst.tolist()], dtype=np.int64)
                 normals = np.zeros((m, ndim), dtype=np.float64)
-                for i, c in enumerate(lst.tolist()):
-                    d = last[c]
-                    normals[i, d // 2] = 1.0 if d & 1 else -1.0
+                normals[np.arange(m), dl // 2] = np.where(dl & 1, 1.0, -1.0)
                 surfaces[sname] = {"cells": lst, "normals": normals}
                 e = entries[dname]
                 if isinstance(e, dict) and e.get("type") == "periodic" and not e.get("generateBndry", True):
@@ -207,3 +205,73 @@ def grid_tables(config: Dict) -> GridTables:
         lib.lbm_grid_destroy(h)
     return GridTables(ndim=ndim, centers=centers, nghbr=nghbr, surfaces=surfaces, bbox=box, cell_length=float(cl.value),
                       max_lvl=level)
+
+
+# box-engine face kinds for the reference's boundary types, plus the kinds the
+# box engine adds for the 3D configurations (the reference has no free-slip,
+# velocity-inlet or zero-gradient-outlet condition)
+BOX_FACES = {"wall": "wall", "periodic": "periodic", "freeslip": "freeslip", "inlet": "open", "outlet": "open"}
+CELL_FLUID, CELL_SOLID, CELL_INLET, CELL_OUTLET = 0, 1, 2, 3
+
+
+def box_case(grid: GridTables, config: Dict) -> Dict:
+    """The dense-box form of a grid built from a config whose domain is one
+    box (objects subtracted from it become solid cells): shape, per-cell flags
+    (x fastest), face kinds, inlet velocity, and for each grid cell its index
+    in the box.  The box spans every cell of the grid, cut layer included, so
+    a "wall" face bounces back half a cell beyond the outermost cells, where
+    the reference's halfway bounce-back at its wet boundary rows puts the
+    wall; a removed cell is solid and bounces back the same way.
+
+    Face entries of the domain box in ``solver.boundary``: ``"wall"`` (no
+    moving-wall value), ``"periodic"``, and the box engine's ``"freeslip"``,
+    ``"inlet"`` (``"velocity"``: equilibrium inflow, -x face) and
+    ``"outlet"`` (zero gradient, +x face)."""
+    ndim = grid.ndim
+    if ndim < 2:
+        raise ConfigError("the box engine needs a 2D or 3D grid")
+    geometry = config.get("geometry", {})
+    domains = [n for n in sorted(geometry) if geometry[n]["type"] == "box" and not geometry[n].get("subtract", False)]
+    if len(domains) != 1:
+        raise ConfigError(f"one domain box expected, found {domains}")
+    dom = domains[0]
+    h = grid.cell_length
+    c = grid.centers
+    rel = (c - c.min(axis=0)) / h
+    k = np.rint(rel).astype(np.int64)
+    if np.abs(rel - k).max() > 1e-6:
+        raise ConfigError("cell centres are not on one uniform lattice")
+    ext = k.max(axis=0) + 1
+    shape = (int(ext[0]), int(ext[1]), int(ext[2]) if ndim == 3 else 1)
+    kz = k[:, 2] if ndim == 3 else np.zeros(len(k), dtype=np.int64)
+    index = k[:, 0] + shape[0] * (k[:, 1] + shape[1] * kz)
+    flags = np.full(shape[0] * shape[1] * shape[2], CELL_SOLID, dtype=np.uint8)
+    flags[index] = CELL_FLUID
+    entries = config.get("solver", {}).get("boundary", {}).get(dom, {})
+    faces, inlet = [], (0.0, 0.0, 0.0)
+    for d, name in enumerate(("-x", "+x", "-y", "+y", "-z", "+z")):
+        if d >= 2 * ndim:
+            faces.append("wall")  # a 2D lattice has no z links
+            continue
+        e = entries.get(name, entries.get("all"))
+        if e is None:
+            raise ConfigError(f'domain box "{dom}": no boundary for face {name}')
+        kind = e.get("type")
+        if kind not in BOX_FACES:
+            raise ConfigError(f'domain box "{dom}", face {name}: type "{kind}" has no box-engine form')
+        if kind == "wall" and any(key in e for key in ("value", "velocity", "tangentialVelocity")):
+            raise ConfigError(f'domain box "{dom}", face {name}: moving walls are set through wall_velocity')
+        if kind == "inlet":
+            if name != "-x":
+                raise ConfigError("the inlet is the -x face")
+            v = [float(x) for x in e.get("velocity", [0.0] * ndim)]
+            inlet = tuple(v + [0.0] * (3 - len(v)))
+            plane = flags.reshape(shape[2], shape[1], shape[0])[:, :, 0]
+            plane[plane == CELL_FLUID] = CELL_INLET
+        if kind == "outlet":
+            if name != "+x":
+                raise ConfigError("the outlet is the +x face")
+            plane = flags.reshape(shape[2], shape[1], shape[0])[:, :, -1]
+            plane[plane == CELL_FLUID] = CELL_OUTLET
+        faces.append(BOX_FACES[kind])
+    return {"shape": shape, "flags": flags, "faces": tuple(faces), "inlet": inlet, "index": index}

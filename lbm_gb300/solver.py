@@ -351,6 +351,16 @@ class LBMSolver:
         self.diverged = False
         self.output_dir = "."
 
+    @classmethod
+    def from_config(cls, config: dict, device: int = 0) -> "LBMSolver":
+        """The solver for a whole reference JSON config: the grid tables are
+        built natively from its grid keys, geometry and boundary block
+        (:func:`lbm_gb300.gridgen.grid_tables`), as the reference's grid
+        generator and CartesianGrid build them."""
+        from .gridgen import grid_tables
+
+        return cls(config["solver"], grid_tables(config), device=device)
+
     def run(self, max_steps: Optional[int] = None) -> Dict:
         """The iteration loop of ``LBMSolver::run``: at iteration t the convergence
         check (every conv_interval, decisive from t > 1), then the time step, then

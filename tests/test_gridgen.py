@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import caseio
+from helpers import channel_sphere_config
 from lbm_gb300 import gridgen
 from lbm_gb300.refconfig import ConfigError
 
@@ -146,3 +147,27 @@ def test_config_errors():
     del bad["solver"]["boundary"]["box"]["+x"]
     with pytest.raises(ConfigError):
         gridgen.grid_tables(bad)
+
+
+def test_box_case_of_a_3d_json_config():
+    cfg = channel_sphere_config()
+    g = gridgen.grid_tables(cfg)
+    b = gridgen.box_case(g, cfg)
+    # x: the longest axis, spanned exactly; y, z: the cut layer adds a row each side
+    assert b["shape"] == (32, 18, 18)
+    assert b["faces"] == ("open", "open", "freeslip", "freeslip", "freeslip", "freeslip")
+    assert b["inlet"] == (0.05, 0.0, 0.0)
+    assert len(np.unique(b["index"])) == g.ncells
+    fl = b["flags"].reshape(18, 18, 32)
+    assert (fl[:, :, 0] == gridgen.CELL_INLET).all() and (fl[:, :, -1] == gridgen.CELL_OUTLET).all()
+    solid = np.argwhere(fl == gridgen.CELL_SOLID)
+    # the solid cells are those the sphere covers whole: all eight vertices inside
+    assert len(solid) > 0
+    for z, y, x in solid:
+        corners = np.array([[x + dx, y - 1 + dy, z - 1 + dz] for dx in (0, 1) for dy in (0, 1) for dz in (0, 1)], dtype=float)
+        assert (np.linalg.norm(corners - [10.0, 8.0, 8.0], axis=1) <= 3.0).all()
+    assert (fl != gridgen.CELL_SOLID).sum() == g.ncells
+    with pytest.raises(ConfigError):
+        bad = json.loads(json.dumps(cfg))
+        bad["solver"]["boundary"]["channel"]["+y"] = {"type": "pressure"}
+        gridgen.box_case(g, bad)

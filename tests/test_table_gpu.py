@@ -6,12 +6,15 @@ the populations (the engine is built to reproduce the reference bit for bit,
 and the test also records whether it does), on the variables, and on the
 residual, whose FP64 summation order differs from the reference's loop.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
 import caseio
 from helpers import load_case, rel_l2
-from lbm_gb300.solver import TableSolver
+from lbm_gb300.solver import LBMSolver, TableSolver
 from lbm_gb300._lib import LBMError
 
 pytestmark = pytest.mark.gpu
@@ -34,6 +37,24 @@ def test_table_engine_matches_reference(name):
     assert np.allclose(r, out["residual"], rtol=TOL, atol=1e-300)
     # the engine keeps the reference's operation order: populations are bitwise equal
     assert np.array_equal(fold, out["fold"]), f"max diff {np.abs(fold - out['fold']).max():.3e}"
+
+
+GRID_CONFIGS = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "grid_configs.json")))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_run_from_json_config_alone(name):
+    """The reference's JSON config alone (grid keys, geometry, solver block):
+    the native grid build (lbm_gb300.gridgen) feeds the GPU engine, and the
+    populations after the fixture's steps equal the reference's bit for bit."""
+    meta, solver, _, out = caseio.load(name)
+    cfg = dict(GRID_CONFIGS[name.rsplit("_", 1)[0]])
+    cfg["solver"] = solver
+    s = LBMSolver.from_config(cfg)
+    s.gpu.initial_condition()
+    s.gpu.step(meta["steps"])
+    assert np.array_equal(s.gpu.populations(), out["fold"])
+    assert rel_l2(s.gpu.vars(), out["vars"]) <= TOL
 
 
 def test_chunked_stepping_equals_one_call():
