@@ -111,6 +111,10 @@ int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selecte
  * (lbm_gpu_box_select_kernel sets both, and reports -1 when they differ). */
 int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd);
 
+/* Run nsteps exactly as lbm_gpu_step does (captured per-parity graphs, the
+ * last two steps recording the residual) with one CUDA event pair around the
+ * whole sequence on the context's stream: *ms is its device time. */
+int lbm_gpu_box_time_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* ms);
 /* Run nsteps exactly as lbm_gpu_step does, but with a CUDA event pair around
  * every launch of the step kernel on the context's stream: total_ms is the
  * device time of the whole sequence, kernel_ms the summed duration of the

@@ -90,6 +90,7 @@ _SIGS = {
     "lbm_gpu_residual_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
     "lbm_gpu_box_profile_steps": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_int64)]),
+    "lbm_gpu_box_time_steps": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double)]),
 }
 
 

@@ -947,7 +947,8 @@ cudaError_t box_initial_condition(BoxState* b, cudaStream_t s) {
   return cudaStreamSynchronize(s);
 }
 
-int box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
+// Enqueue nsteps on stream s (no synchronisation).
+int box_step_enqueue(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
   // All but the last two steps replay a captured one-step graph per parity.
   // The last two record the moments (mode 1) and then the residual partials
   // against them (mode 2), so lbm_gpu_residual is ready after any call of two
@@ -982,6 +983,12 @@ int box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
     b->mom_valid = 1;
     b->res_ready = mom == 2;
   }
+  return LBM_OK;
+}
+
+int box_step(BoxState* b, int64_t nsteps, cudaStream_t s, std::string& err) {
+  const int rc = box_step_enqueue(b, nsteps, s, err);
+  if(rc != LBM_OK) return rc;
   cudaError_t e = cudaStreamSynchronize(s);
   if(e != cudaSuccess) return cerr(err, e, "step sync");
   return check_wait_flag(b, err);
@@ -1508,6 +1515,32 @@ int lbm_gpu_box_probe(lbm_gpu_ctx* ctx, const int64_t* cells, int64_t n, double*
     lbm_internal_set_error(ctx, std::string("box probe: ") + cudaGetErrorString(e));
     return LBM_ERR_CUDA;
   }
+  return LBM_OK;
+}
+
+int lbm_gpu_box_time_steps(lbm_gpu_ctx* ctx, int64_t nsteps, double* ms) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b || nsteps < 0 || !ms) return LBM_ERR_INVALID;
+  cudaStream_t s = lbm_internal_stream(ctx);
+  cudaEvent_t  ev[2];
+  cudaEventCreate(&ev[0]);
+  cudaEventCreate(&ev[1]);
+  cudaEventRecord(ev[0], s);
+  std::string err;
+  int         rc = box_step_enqueue(b, nsteps, s, err);
+  cudaEventRecord(ev[1], s);
+  cudaError_t e = cudaEventSynchronize(ev[1]);
+  float       t = 0;
+  if(e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if(rc == LBM_OK && e != cudaSuccess) rc = cerr(err, e, "time steps");
+  if(rc == LBM_OK) rc = check_wait_flag(b, err);
+  if(rc != LBM_OK) {
+    lbm_internal_set_error(ctx, err);
+    return rc;
+  }
+  *ms = t;
   return LBM_OK;
 }
 

@@ -275,6 +275,13 @@ class BoxSolver:
               "profile_steps")
         return tot.value, ker.value, cnt.value
 
+    def time_steps(self, n: int) -> float:
+        """Run n steps as :meth:`step` does; returns their device time in ms
+        (one CUDA event pair on the engine's stream around the whole run)."""
+        ms = C.c_double()
+        check(self._lib.lbm_gpu_box_time_steps(self.ctx, int(n), C.byref(ms)), self.ctx, "time_steps")
+        return ms.value
+
     def threads_per_block(self) -> int:
         t = C.c_int32()
         check(self._lib.lbm_gpu_box_autotune(self.ctx, C.byref(t)), self.ctx, "autotune")

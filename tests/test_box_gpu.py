@@ -325,3 +325,16 @@ def test_3d_json_config_runs_on_the_box_engine():
     g.step(40)
     o.step(40)
     assert rel_l2(g.populations(), o.populations()) <= TOL
+
+
+def test_timed_steps_equal_plain_steps():
+    """lbm_gpu_box_time_steps runs the same step sequence as lbm_gpu_step."""
+    a, _ = make_pair("d3q19_sphere_open", "f16dev")
+    b, _ = make_pair("d3q19_sphere_open", "f16dev")
+    for s in (a, b):
+        s.initial_condition()
+    a.step(23)
+    ms = b.time_steps(23)
+    assert ms > 0
+    assert np.array_equal(a.populations(), b.populations())
+    np.testing.assert_array_equal(a.residual(), b.residual())
