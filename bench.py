@@ -297,6 +297,33 @@ def warmstart_run(args):
                        "per_reynolds_number": args.ws_per_batch}, "detail": out}
 
 
+def grid_run(args):
+    """Grid and tables of the D3Q19 sphere channel (512 x 256 x 256 box with
+    a subtracted sphere of radius 24, level 9) built from the JSON config:
+    the host build and the device build (same tables, checked), wall time."""
+    from lbm_gb300 import gridgen
+
+    cfg = {"dim": 3, "partitionLevel": 9, "uniformLevel": 9, "maxRfnmtLvl": 9,
+           "geometry": {"channel": {"type": "box", "A": [0, 0, 0], "B": [512, 256, 256], "body": "flow"},
+                        "sphere": {"type": "sphere", "center": [128, 128, 128], "radius": 24, "body": "flow", "subtract": True}},
+           "solver": {"boundary": {"channel": {"-x": {"type": "inlet", "velocity": [0.05, 0, 0]}, "+x": {"type": "outlet"},
+                                               "-y": {"type": "freeslip"}, "+y": {"type": "freeslip"},
+                                               "-z": {"type": "freeslip"}, "+z": {"type": "freeslip"}},
+                                   "sphere": {"all": {"type": "wall"}}}}}
+    gridgen.grid_tables(cfg, device=0)  # warm-up: context and module load
+    t0 = time.perf_counter()
+    dev = gridgen.grid_tables(cfg, device=0)
+    t_dev = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    host = gridgen.grid_tables(cfg)
+    t_host = time.perf_counter() - t0
+    same = bool(np.array_equal(dev.centers, host.centers) and np.array_equal(dev.nghbr, host.nghbr) and
+                all(np.array_equal(dev.surfaces[k]["cells"], host.surfaces[k]["cells"]) for k in host.surfaces))
+    return {"metric": "grid and table build, D3Q19 sphere channel 512x256x256 from its JSON config", "value": t_dev, "unit": "s",
+            "higher_is_better": False, "config": {"workload": "uniform level 9, box minus sphere r=24", "cells": dev.ncells},
+            "host_s": t_host, "device_s": t_dev, "identical": same}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,7 +332,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
@@ -335,7 +362,8 @@ def main():
         args.warmup = 3
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
-            fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run}[args.workload]
+            fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
+                  "grid": grid_run}[args.workload]
             print(json.dumps(fn(args)))
         return
 

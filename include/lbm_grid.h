@@ -29,8 +29,8 @@
  * edge neighbours are formed through the main neighbours (x step first,
  * then y, then z), indexed in the D3Q19 direction order.
  *
- * All calls are host-only (no device memory, no CUDA call).  Status codes
- * are those of lbm_gpu.h.
+ * All calls but lbm_grid_create_device are host-only (no device memory, no
+ * CUDA call).  Status codes are those of lbm_gpu.h.
  */
 #ifndef LBM_GRID_H
 #define LBM_GRID_H
@@ -66,6 +66,17 @@ typedef struct lbm_grid lbm_grid;
  * neighbours.  Objects are given in the order of the config's "geometry"
  * keys (sorted). */
 int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int32_t nobj, const double* bbox, lbm_grid** out);
+
+/* lbm_grid_create with the cells enumerated on GPU `device`: the curve
+ * indices of the level are walked in order (the index is a bijection of the
+ * positions), each position tested with the host's geometry code, and the
+ * kept cells numbered by a prefix sum; main neighbours and boundary cells are
+ * found on the device too.  The grid equals lbm_grid_create's bit for bit.
+ * Needs ndim*level <= 30 (one byte and one int32 of device memory per
+ * position of the level's cube, plus the cell tables); everything after
+ * creation runs on the host as for lbm_grid_create. */
+int lbm_grid_create_device(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int32_t nobj, const double* bbox, int32_t device,
+                           lbm_grid** out);
 
 /* "alignNodesWithSurface": stretch the grid so that the outermost cell
  * centres along `align_dir` (along every axis when the centres span the same

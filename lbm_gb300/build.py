@@ -36,6 +36,8 @@ UNITS = {
     # host-only grid and table build: no floating-point contraction, so that
     # the cut tests round as the reference's do on either host architecture
     "grid.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    # its device counterpart: the same geometry code, no contraction either
+    "grid_device.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

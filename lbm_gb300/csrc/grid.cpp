@@ -23,6 +23,8 @@
 // floating-point contraction so that the host compilers of both machines
 // round the same way.
 #include "../../include/lbm_grid.h"
+#include "grid_geom.h"
+#include "grid_internal.h"
 
 #include <algorithm>
 #include <cmath>
@@ -33,112 +35,13 @@
 #include <unordered_map>
 #include <vector>
 
-struct lbm_grid {
-  int                        D = 0, level = 0;
-  std::vector<lbm_geom_desc> objs;
-  std::vector<std::vector<int>> bodies;  // object ids per body, in first-appearance order
-  double                     bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0}, cog[3] = {0, 0, 0};
-  double                     len0 = 0, cell_length = 0;
-  double                     cut_length = 0;  // length of the generator's cut tests (differs after alignment)
-  int64_t                    lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};  // candidate position range
-  int64_t                    n = 0;
-  std::vector<double>        centers;    // n x D
-  std::vector<int32_t>       ipos;       // n x D integer positions on the level
-  std::vector<int64_t>       nbr;        // n x 2D main neighbours
-  std::vector<uint8_t>       bndry;      // boundary property
-  std::vector<int64_t>       bcells;     // the boundary cells, ascending
-  std::vector<uint8_t>       assigned;   // per cell: bit d set when (cell, d) belongs to a surface
-};
+namespace lbm_grid_impl {
 
-namespace {
+using namespace lbm_grid_geom;
 
-// gcem::sqrt(2) as the reference's constexpr evaluation rounds it (one unit in
-// the last place below the correctly rounded square root); used by the 2D
-// sphere cut test (src/geometry.h:667).
-constexpr double kSqrt2Ref = 0x1.6a09e667f3bccp+0;
-constexpr double kEps      = std::numeric_limits<double>::epsilon();
+bool geom_inside(const lbm_grid& g, const double* x) { return set_inside(g.geom(), x, g.D); }
 
-// Euclidean norm of a - b summed in axis order (Eigen's squaredNorm of a
-// small fixed-size vector), then sqrt
-double dist(const double* a, const double* b, int D) {
-  double s = 0.0;
-  for(int d = 0; d < D; ++d) {
-    const double t = a[d] - b[d];
-    s              = d == 0 ? t * t : s + t * t;
-  }
-  return std::sqrt(s);
-}
-
-// GeomBox::pointIsInside / GeomSphere::pointIsInside (src/geometry.h:660-662, 755-762)
-bool obj_inside(const lbm_geom_desc& o, const double* x, int D) {
-  if(o.kind == LBM_GEOM_SPHERE) return dist(x, o.center, D) < o.radius + kEps;
-  for(int d = 0; d < D; ++d)
-    if(o.a[d] > x[d] || o.b[d] < x[d]) return false;
-  return true;
-}
-
-// GeomBox::cutWithCell (src/geometry.h:764-807); the 3D form extends the 2D
-// rule to the six faces
-bool box_cut(const lbm_geom_desc& o, const double* c, double len, int D) {
-  const double h = 0.5 * len;
-  if(D == 1) return std::abs(o.a[0] - c[0]) <= h || std::abs(o.b[0] - c[0]) <= h;
-  for(int a = 0; a < D; ++a) {
-    bool span = true;  // within the face's extent along the other axes
-    for(int b = 0; b < D; ++b)
-      if(b != a && !(o.a[b] - h <= c[b] && o.b[b] + h >= c[b])) span = false;
-    if(!span) continue;
-    if(std::abs(c[a] - o.a[a]) <= h) return true;
-    if(std::abs(c[a] - o.b[a]) <= h) return true;
-  }
-  return false;
-}
-
-// GeomSphere::cutWithCell (src/geometry.h:664-698): a cell within the
-// annulus of the circumscribed radius is cut unless all its vertices lie in
-// the sphere.  3D: circumscribed radius sqrt(3) h and eight vertices.
-bool sphere_cut(const lbm_geom_desc& o, const double* c, double len, int D) {
-  const double distance = dist(c, o.center, D);
-  const double h        = 0.5 * len;
-  const double surr     = (D == 3 ? std::sqrt(3.0) : kSqrt2Ref) * h;
-  if(!(distance <= o.radius + surr && distance >= o.radius - surr)) return false;
-  if(D == 1) return true;  // the reference's vertex count stays 0 below 2D
-  double origin[3];
-  for(int d = 0; d < D; ++d) origin[d] = c[d] - h;
-  int inside = 0;
-  for(int v = 0; v < (1 << D); ++v) {
-    double vert[3];
-    for(int d = 0; d < D; ++d) vert[d] = ((v >> d) & 1) ? origin[d] + len : origin[d];
-    if(dist(vert, o.center, D) <= o.radius) ++inside;
-  }
-  return inside < (1 << D);
-}
-
-bool obj_cut(const lbm_geom_desc& o, const double* c, double len, int D) {
-  return o.kind == LBM_GEOM_SPHERE ? sphere_cut(o, c, len, D) : box_cut(o, c, len, D);
-}
-
-// GeometryManager::pointIsInside (src/geometry.h:1011-1047)
-bool geom_inside(const lbm_grid& g, const double* x) {
-  for(const auto& body : g.bodies) {
-    bool has_sub = false;
-    for(int i : body) has_sub |= g.objs[i].subtract != 0;
-    for(int i : body) {
-      if(!obj_inside(g.objs[i], x, g.D)) continue;
-      if(!has_sub) return true;
-      if(g.objs[i].subtract) return false;
-      for(int j : body)
-        if(g.objs[j].subtract && obj_inside(g.objs[j], x, g.D)) return false;
-      return true;
-    }
-  }
-  return false;
-}
-
-bool geom_cut(const lbm_grid& g, const double* c, double len) {
-  for(const auto& o : g.objs)
-    if(obj_cut(o, c, len, g.D)) return true;
-  return false;
-}
+bool geom_cut(const lbm_grid& g, const double* c, double len) { return set_cut(g.geom(), c, len, g.D); }
 
 // hilbert::index (include/common/math/hilbert.h:16-48) of a position in the
 // unit cube
@@ -180,59 +83,54 @@ void link_cells(lbm_grid& g) {
       if(m >= 0) g.nbr[c * M + dir] = m;
     }
   g.bndry.assign(g.n, 0);
-  g.assigned.assign(g.n, 0);
   for(int64_t c = 0; c < g.n; ++c) {
     if(!geom_cut(g, &g.centers[c * D], g.cell_length)) continue;
     int present = 0;
     for(int dir = 0; dir < M; ++dir) present += g.nbr[c * M + dir] != -1;
     g.bndry[c] = present < M;
   }
+  list_boundary_cells(g);
+}
+
+void list_boundary_cells(lbm_grid& g) {
+  g.assigned.assign(g.n, 0);
   g.bcells.clear();
   for(int64_t c = 0; c < g.n; ++c)
     if(g.bndry[c]) g.bcells.push_back(c);
 }
 
-}  // namespace
-
-extern "C" {
-
-int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int32_t nobj, const double* bbox, lbm_grid** out) {
-  if(!out) return LBM_ERR_INVALID;
-  *out = nullptr;
+int setup(lbm_grid& g, int ndim, int level, const lbm_geom_desc* objs, int nobj, const double* bbox) {
   if(ndim < 1 || ndim > 3 || level < 1 || level > 20 || nobj < 0 || (nobj > 0 && !objs) || (nobj == 0 && !bbox))
     return LBM_ERR_INVALID;
-  if(static_cast<int64_t>(ndim) * level > 62) return LBM_ERR_INVALID;
   for(int i = 0; i < nobj; ++i)
     if(objs[i].kind != LBM_GEOM_BOX && objs[i].kind != LBM_GEOM_SPHERE) return LBM_ERR_UNSUPPORTED;
-  lbm_grid* g = new(std::nothrow) lbm_grid();
-  if(!g) return LBM_ERR_NOMEM;
   const int D = ndim;
-  g->D        = D;
-  g->level    = level;
-  g->objs.assign(objs, objs + nobj);
+  g.D         = D;
+  g.level     = level;
+  g.objs.assign(objs, objs + nobj);
+  // bodies numbered in order of first appearance
+  std::vector<int32_t> ids;
+  g.body.assign(nobj, 0);
   for(int i = 0; i < nobj; ++i) {
-    bool placed = false;
-    for(auto& b : g->bodies)
-      if(g->objs[b[0]].body == objs[i].body) {
-        b.push_back(i);
-        placed = true;
-      }
-    if(!placed) g->bodies.push_back({i});
+    const auto it = std::find(ids.begin(), ids.end(), objs[i].body);
+    g.body[i]     = static_cast<int32_t>(it - ids.begin());
+    if(it == ids.end()) ids.push_back(objs[i].body);
   }
+  g.nbody = static_cast<int>(ids.size());
   // bounding box: given, or the union of the objects' boxes
   // (GeometryManager::getBoundingBox, src/geometry.h:1080-1103)
   for(int d = 0; d < D; ++d) {
     if(bbox) {
-      g->bmin[d] = bbox[2 * d];
-      g->bmax[d] = bbox[2 * d + 1];
+      g.bmin[d] = bbox[2 * d];
+      g.bmax[d] = bbox[2 * d + 1];
       continue;
     }
     for(int i = 0; i < nobj; ++i) {
       const lbm_geom_desc& o  = objs[i];
       const double         lo = o.kind == LBM_GEOM_SPHERE ? o.center[d] - o.radius : o.a[d];
       const double         hi = o.kind == LBM_GEOM_SPHERE ? o.center[d] + o.radius : o.b[d];
-      if(i == 0 || g->bmin[d] > lo) g->bmin[d] = lo;
-      if(i == 0 || g->bmax[d] < hi) g->bmax[d] = hi;
+      if(i == 0 || g.bmin[d] > lo) g.bmin[d] = lo;
+      if(i == 0 || g.bmax[d] < hi) g.bmax[d] = hi;
     }
   }
   // extents, decisive direction, centre and level lengths
@@ -240,59 +138,79 @@ int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int3
   int    dec = 0;
   double ext[3];
   for(int d = 0; d < D; ++d) {
-    ext[d] = std::abs(g->bmax[d] - g->bmin[d]);
-    dec    = ext[d] > ext[dec] ? d : dec;
-    g->cog[d] = g->bmin[d] + 0.5 * (g->bmax[d] - g->bmin[d]);
+    ext[d]   = std::abs(g.bmax[d] - g.bmin[d]);
+    dec      = ext[d] > ext[dec] ? d : dec;
+    g.cog[d] = g.bmin[d] + 0.5 * (g.bmax[d] - g.bmin[d]);
   }
-  g->len0 = (1.0 + 1.0 / std::ldexp(1.0, 100)) * ext[dec];
+  g.len0 = (1.0 + 1.0 / std::ldexp(1.0, 100)) * ext[dec];
   std::vector<double> len(level + 1);
-  len[0] = g->len0;
+  len[0] = g.len0;
   for(int l = 1; l <= level; ++l) len[l] = 0.5 * len[l - 1];
-  g->cell_length = len[level];
-  if(!(g->cell_length > 0.0)) {
-    delete g;
-    return LBM_ERR_INVALID;
-  }
+  g.cell_length = len[level];
+  g.cut_length  = g.cell_length;
+  if(!(g.cell_length > 0.0)) return LBM_ERR_INVALID;
   // centre coordinate of position i along an axis: the root centre plus the
   // child offsets level by level (refineCell,
   // src/gridgenerator/cartesiangrid_generation.h:419-451)
-  const int64_t       side = int64_t(1) << level;
-  std::vector<double> cv[3];
-  int64_t             lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  const int64_t side = int64_t(1) << level;
   for(int d = 0; d < D; ++d) {
-    cv[d].resize(side);
+    g.cv[d].resize(side);
     for(int64_t i = 0; i < side; ++i) {
-      double c = g->cog[d];
+      double c = g.cog[d];
       for(int l = 0; l < level; ++l) c = c + (0.5 * len[l + 1]) * (((i >> (level - 1 - l)) & 1) ? 1.0 : -1.0);
-      cv[d][i] = c;
+      g.cv[d][i] = c;
     }
     // candidate range: a cell further than one cell length from the bounding
-    // box is neither cut nor inside
-    lo[d] = side;
-    hi[d] = -1;
-    for(int64_t i = 0; i < side; ++i)
-      if(cv[d][i] >= g->bmin[d] - g->cell_length && cv[d][i] <= g->bmax[d] + g->cell_length) {
-        lo[d] = std::min(lo[d], i);
-        hi[d] = std::max(hi[d], i);
-      }
-    if(hi[d] < lo[d]) {
-      delete g;
-      return LBM_ERR_INVALID;
+    // box and from every object's box is neither cut nor inside
+    double umin = g.bmin[d], umax = g.bmax[d];
+    for(int i = 0; i < nobj; ++i) {
+      const lbm_geom_desc& o = objs[i];
+      umin = std::min(umin, o.kind == LBM_GEOM_SPHERE ? o.center[d] - o.radius : std::min(o.a[d], o.b[d]));
+      umax = std::max(umax, o.kind == LBM_GEOM_SPHERE ? o.center[d] + o.radius : std::max(o.a[d], o.b[d]));
     }
+    int64_t lo = side, hi = -1;
+    for(int64_t i = 0; i < side; ++i)
+      if(g.cv[d][i] >= umin - g.cell_length && g.cv[d][i] <= umax + g.cell_length) {
+        lo = std::min(lo, i);
+        hi = std::max(hi, i);
+      }
+    if(hi < lo) return LBM_ERR_INVALID;
+    g.lo[d]  = lo;
+    g.ext[d] = hi - lo + 1;
   }
+  return LBM_OK;
+}
+
+}  // namespace lbm_grid_impl
+
+using namespace lbm_grid_impl;
+
+extern "C" {
+
+int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int32_t nobj, const double* bbox, lbm_grid** out) {
+  if(!out) return LBM_ERR_INVALID;
+  *out = nullptr;
+  lbm_grid* g = new(std::nothrow) lbm_grid();
+  if(!g) return LBM_ERR_NOMEM;
+  int rc = setup(*g, ndim, level, objs, nobj, bbox);
+  if(rc != LBM_OK) {
+    delete g;
+    return rc;
+  }
+  const int D = ndim;
   // kept cells: cut by an object, or centre inside the geometry
   struct Kept {
     uint64_t key;
     int32_t  p[3];
   };
   std::vector<Kept> kept;
-  const int64_t     nx = hi[0] - lo[0] + 1, ny = D > 1 ? hi[1] - lo[1] + 1 : 1, nz = D > 2 ? hi[2] - lo[2] + 1 : 1;
+  const int64_t     nx = g->ext[0], ny = g->ext[1], nz = g->ext[2];
   for(int64_t k = 0; k < nz; ++k)
     for(int64_t j = 0; j < ny; ++j)
       for(int64_t i = 0; i < nx; ++i) {
-        const int64_t p[3] = {lo[0] + i, D > 1 ? lo[1] + j : 0, D > 2 ? lo[2] + k : 0};
+        const int64_t p[3] = {g->lo[0] + i, D > 1 ? g->lo[1] + j : 0, D > 2 ? g->lo[2] + k : 0};
         double        c[3];
-        for(int d = 0; d < D; ++d) c[d] = cv[d][p[d]];
+        for(int d = 0; d < D; ++d) c[d] = g->cv[d][p[d]];
         if(!(geom_cut(*g, c, g->cell_length) || geom_inside(*g, c))) continue;
         // curve index of the centre in the unit cube of the root cell
         // (reorderHilbertCurve, cartesiangrid_generation.h:677-680)
@@ -317,13 +235,8 @@ int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int3
   for(int64_t c = 0; c < n; ++c)
     for(int d = 0; d < D; ++d) {
       g->ipos[c * D + d]    = kept[c].p[d];
-      g->centers[c * D + d] = cv[d][kept[c].p[d]];
+      g->centers[c * D + d] = g->cv[d][kept[c].p[d]];
     }
-  for(int d = 0; d < 3; ++d) g->lo[d] = lo[d];
-  g->ext[0]     = nx;
-  g->ext[1]     = ny;
-  g->ext[2]     = nz;
-  g->cut_length = g->cell_length;
   link_cells(*g);
   *out = g;
   return LBM_OK;

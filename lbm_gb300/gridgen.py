@@ -33,7 +33,7 @@ reference cannot build, follows the same rules (include/lbm_grid.h).
 from __future__ import annotations
 
 import ctypes as C
-from typing import Dict, List
+from typing import Dict, List, Optional
 
 import numpy as np
 
@@ -52,6 +52,8 @@ class GeomDesc(C.Structure):
 
 _SIGS = {
     "lbm_grid_create": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "lbm_grid_create_device": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                         C.POINTER(C.c_void_p)]),
     "lbm_grid_align": (C.c_int, [C.c_void_p, C.c_int32]),
     "lbm_grid_curve_index": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_uint64)]),
     "lbm_grid_ncells": (C.c_int64, [C.c_void_p]),
@@ -118,9 +120,10 @@ def geometry_objects(geometry: Dict, ndim: int):
     return descs, names
 
 
-def grid_tables(config: Dict) -> GridTables:
+def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
     """The reference's LBM grid tables for a JSON config (the grid generator's
-    keys plus ``solver.boundary``)."""
+    keys plus ``solver.boundary``).  With ``device`` the cells are enumerated
+    on that GPU (``lbm_grid_create_device``, the same tables)."""
     ndim = int(config.get("dim", 0))
     if ndim not in (1, 2, 3):
         raise ConfigError(f"dim must be 1, 2 or 3, got {ndim}")
@@ -136,8 +139,11 @@ def grid_tables(config: Dict) -> GridTables:
         bbox = (C.c_double * (2 * ndim))(*[float(x) for x in config.get("boundingBox", default)])
     lib = _grid_lib()
     h = C.c_void_p()
-    rc = lib.lbm_grid_create(ndim, level, C.cast(descs, C.c_void_p), len(names), C.cast(bbox, C.c_void_p) if bbox else None,
-                             C.byref(h))
+    pb = C.cast(bbox, C.c_void_p) if bbox else None
+    if device is None:
+        rc = lib.lbm_grid_create(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, C.byref(h))
+    else:
+        rc = lib.lbm_grid_create_device(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, int(device), C.byref(h))
     _lib.check(rc, what="lbm_grid_create")
     try:
         if config.get("alignNodesWithSurface", False):
