@@ -324,6 +324,45 @@ def grid_run(args):
             "host_s": t_host, "device_s": t_dev, "identical": same}
 
 
+def lpt_run(args):
+    """Particle step of the reference's falling1m case on the GPU: 10^6
+    particles, 2D, the reference's default force model (gravity, buoyancy,
+    Stokes drag) with forward Euler, dt 1e-7, 100 steps per call (one launch;
+    the state stays in registers).  CPU baseline: the oracle's scalar
+    restatement on a 1,000-particle sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lpt_oracle as lo
+    from lbm_gb300.lpt import ParticleSolver
+
+    n, steps = 1_000_000, 100
+    rng = np.random.default_rng(123456789)
+    v = np.full((n, 11), np.nan)
+    v[:, :2] = rng.uniform(0.0, 1.0, (n, 2))
+    v[:, 2:4] = 0.0
+    v[:, 6], v[:, 7], v[:, 9] = 0.01, 800.0, 4.0 / 3.0 * np.pi * 0.01 ** 3
+    solver = {"dt": 1e-7, "gravity": [0, 10]}
+    ps = ParticleSolver.from_config(solver, 2, capacity=n)
+    ps.set_particles(v)
+    ps.step(steps)  # warm-up
+    times = []
+    for _ in range(max(3, args.warmup)):
+        t0 = time.perf_counter()
+        ps.step(steps)
+        times.append(time.perf_counter() - t0)
+    sec = min(times)
+    prm = lo.config_params(solver, 2)
+    sample = v[:1000]
+    t0 = time.perf_counter()
+    lo.step(sample, 2, nsteps=steps, **prm)
+    cpu = 1000 * steps / (time.perf_counter() - t0) / 1e6
+    return {"metric": "particle steps per second (10^6 particles, 2D, gravity + buoyancy + Stokes drag, forward Euler)",
+            "value": n * steps / sec / 1e6, "unit": "M particle-steps/s", "dtype": "f64",
+            "config": {"workload": "falling1m: 1e6 particles, 100 steps per call", "particles": n, "steps_per_call": steps},
+            "ms_per_call": sec * 1e3, "bytes_per_particle_call": 2 * 8 * 11,
+            "cpu_baseline": {"value": cpu, "unit": "M particle-steps/s", "cores": 1, "kind": "port",
+                             "sample": "1,000 particles x 100 steps, scalar Python restatement"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,7 +371,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid"],
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
@@ -363,7 +402,7 @@ def main():
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
-                  "grid": grid_run}[args.workload]
+                  "grid": grid_run, "lpt": lpt_run}[args.workload]
             print(json.dumps(fn(args)))
         return
 

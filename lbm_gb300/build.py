@@ -38,6 +38,8 @@ UNITS = {
     "grid.cpp": ["-Xcompiler", "-ffp-contract=off"],
     # its device counterpart: the same geometry code, no contraction either
     "grid_device.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    # particle step: the reference's separately rounded FP64 operations
+    "lpt.cu": ["-fmad=false"],
 }
 
 

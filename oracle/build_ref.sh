@@ -50,7 +50,11 @@ FLAGS=(-std=c++17 -O3 -fopenmp -w -I"$HERE/mpi_stub" -I"$OUT" -I"$OUT/src" -I"$R
 P1=$!
 "$CXX" "${FLAGS[@]}" -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
 P2=$!
+"$CXX" "${FLAGS[@]}" -c "$HERE/ref_lpt_harness.cpp" -o "$OUT/ref_lpt_harness.o" &
+P3=$!
 wait $P1
 wait $P2
+wait $P3
 "$CXX" -fopenmp "$OUT/gridGenerator.o" "$OUT/ref_harness.o" -o "$OUT/ref_harness" -ldl -lpthread
-echo "built $OUT/ref_harness"
+"$CXX" -fopenmp "$OUT/ref_lpt_harness.o" -o "$OUT/ref_lpt_harness" -ldl -lpthread
+echo "built $OUT/ref_harness $OUT/ref_lpt_harness"

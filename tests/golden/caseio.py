@@ -23,7 +23,23 @@ def fixture_path(name: str) -> str:
 
 
 def list_fixtures():
-    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz"))
+    """The LBM fixtures (the particle solver's are lpt_*)."""
+    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz") and not f.startswith("lpt_"))
+
+
+def list_lpt_fixtures():
+    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz") and f.startswith("lpt_"))
+
+
+def load_lpt(name: str):
+    """meta, solver block, and the reference's particle state (m_vars layout,
+    particles x (3*ndim+5)) before and after ``meta['steps']`` steps, and the
+    start locations."""
+    z = np.load(fixture_path(name), allow_pickle=False)
+    meta = json.loads(str(z["meta"]))
+    solver = json.loads(str(z["solver"]))
+    nv = meta["nvars"]
+    return meta, solver, z["vars0"].reshape(-1, nv), z["vars"].reshape(-1, nv), z["start"].reshape(-1, meta["ndim"])
 
 
 def load(name: str):

@@ -173,6 +173,59 @@ def write_grid_configs():
     print(f"grid_configs.json: {len(out)} cases")
 
 
+# particle solver (src/lpt): the reference's own LPTSolver through
+# oracle/_ref/ref_lpt_harness -> tests/golden/lpt_<case>_<steps>.npz with the
+# particle state before and after (the solver's m_vars layout), the start
+# locations and the constants.  The reference's freefall tests, shortened, and
+# the same case with the other force models (ambient velocity set, so that the
+# drag acts on a moving fluid) and integrators.
+LPT_HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_lpt_harness")
+LPT_MODELS = [("constDensityRatioGrav", "ForwardEuler", 2), ("constDensityRatioGravStokesDrag", "ImplicitEuler", 3),
+              ("constDensityRatioGravNlinDrag", "ImplicitEuler", 2), ("constDensityRatioGravBuo", "ForwardEuler", 3),
+              ("constDensityRatioGravBuoStokesDrag", "ForwardEuler", 2), ("constDensityRatioGravBuoNlinDrag", "ForwardEuler", 3),
+              ("constDensityaGravBuoStokesDrag", "ImplicitEuler", 2), ("constDensityaGravBuoNlinDrag", "ImplicitEuler", 3)]
+LPT_CASES = [(f"lpt_{n}", ("ref", f"test/lpt/{n}.json"), 2000) for n in
+             ("falling", "falling_implicit", "falling_nonlinearDrag", "falling_Buoyancy", "falling_noDrag", "falling3d")]
+
+
+def lpt_model_config(model, integration, dim):
+    base = "falling3d.json" if dim == 3 else "falling.json"
+    with open(os.path.join(REF, "test", "lpt", base)) as fh:
+        cfg = json.load(fh)
+    s = cfg["solver"]
+    s["model"] = model
+    s["integrationMethod"] = integration
+    s["v_infty"] = [0.3, -0.2, 0.1][:dim]
+    s["rho_infty"] = 1.1
+    s["dt"] = 1e-4
+    s["randomvol_pos"]["init_rho_p"] = 50.0
+    s["randomvol_pos"]["init_velo"] = [0.5, 0.25, -0.1][:dim]
+    return cfg
+
+
+def run_lpt(name, cfg, steps):
+    with tempfile.TemporaryDirectory() as tmp:
+        local_cfg = os.path.join(tmp, "case.json")
+        with open(local_cfg, "w") as fh:
+            json.dump(cfg, fh)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        subprocess.run([LPT_HARNESS, local_cfg, str(steps), out], cwd=tmp, check=True, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
+        with open(os.path.join(out, "meta.json")) as fh:
+            meta = json.load(fh)
+        arrays = {k: np.fromfile(os.path.join(out, f"{k}.f64"), dtype=np.float64) for k in ("vars0", "vars", "start")}
+    np.savez_compressed(os.path.join(HERE, f"{name}_{steps}.npz"), meta=json.dumps(meta), solver=json.dumps(cfg["solver"]), **arrays)
+    print(f"{name}_{steps}: {meta['particles']} particles")
+
+
+def write_lpt():
+    for name, src, steps in LPT_CASES:
+        run_lpt(name, load_config(src), steps)
+    for model, integration, dim in LPT_MODELS:
+        run_lpt(f"lpt_{model}_{dim}d", lpt_model_config(model, integration, dim), 2000)
+
+
 # known answers of the reference's curve index (UnitTest/test_hilbert.cpp):
 # every EXPECT_EQ(hilbert::index<N>(point, level), value) with its point ->
 # tests/golden/hilbert_kat.json
@@ -202,6 +255,8 @@ def main(argv):
         write_grid_configs()
     if not wanted or "hilbert_kat" in wanted:
         write_hilbert_kat()
+    if not wanted or "lpt" in wanted:
+        write_lpt()
     for name, src, steps in CASES:
         if wanted and name not in wanted:
             continue
