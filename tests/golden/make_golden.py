@@ -50,6 +50,15 @@ CASES = [
     ("poisson2d_helmholtz_small", ("own", "poisson2d_helmholtz_small.json"), [100]),
     ("cavity_small", ("own", "cavity_small.json"), [1, 100]),
     ("channel_mixed_small", ("own", "channel_mixed_small.json"), [1, 100]),
+    # the reference's remaining Poisson tests and its backward-facing steps
+    # (bodies made of several boxes), at coarser levels
+    ("poisson1D_l8", ("ref", "test/poisson/poisson1D.json", {"partitionLevel": 8, "uniformLevel": 8, "maxRfnmtLvl": 8}), [50]),
+    ("poisson2D_l5", ("ref", "test/poisson/poisson2D.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [50]),
+    ("poisson2D_reaction_l5", ("ref", "test/poisson/poisson2D_reaction.json",
+                               {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [50]),
+    ("poissonD2Q9_l5", ("ref", "test/poisson/poissonD2Q9.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [50]),
+    ("step_ns_l5", ("ref", "test/step/step_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [40]),
+    ("step_poisson_l5", ("ref", "test/step/step_poisson.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [40]),
     # the reference's 2D flow around an obstacle (box minus a circle, pressure
     # inlet / outlet, bounce-back walls) at level 5 instead of 8
     ("sphere_ns_l5", ("ref", "test/sphere/sphere_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}),
