@@ -44,3 +44,28 @@ def test_invalid_arguments_are_rejected_without_a_gpu():
     assert lib.lbm_gpu_create(None, None, None, None) == -1
     assert lib.lbm_gpu_step(None, 1) == -1
     assert lib.lbm_gpu_create_box(None, None, None, None) == -1
+
+
+def test_grid_and_particle_entry_points_reject_invalid_arguments_without_a_gpu():
+    import ctypes as C
+
+    from lbm_gb300 import _lib, gridgen
+    from lbm_gb300.lpt import _lpt_lib
+
+    lib = gridgen._grid_lib()
+    h = C.c_void_p()
+    assert lib.lbm_grid_create(0, 5, None, 0, None, C.byref(h)) == -1           # no dimension
+    assert lib.lbm_grid_create(2, 5, None, 0, None, C.byref(h)) == -1           # no geometry and no box
+    descs, _ = gridgen.geometry_objects({"b": {"type": "box", "A": [0, 0, 0], "B": [1, 1, 1]}}, 3)
+    # 2^33 positions: more than the device build takes; refused before any CUDA call
+    assert lib.lbm_grid_create_device(3, 11, C.cast(descs, C.c_void_p), 1, None, 0, C.byref(h)) == -2
+    bad = gridgen.GeomDesc()
+    bad.kind = 7
+    assert lib.lbm_grid_create(2, 3, C.byref(bad), 1, None, C.byref(h)) == -2   # unknown object kind
+    assert lib.lbm_grid_align(None, 0) == -1
+    assert lib.lbm_grid_ncells(None) == 0
+    lp = _lpt_lib()
+    assert lp.lbm_lpt_create(None, C.byref(h)) == -1
+    assert lp.lbm_lpt_step(None, 1) == -1
+    assert lp.lbm_lpt_set_particles(None, 0, None) == -1
+    assert lp.lbm_lpt_count(None) == 0

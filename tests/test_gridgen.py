@@ -171,3 +171,27 @@ def test_box_case_of_a_3d_json_config():
         bad = json.loads(json.dumps(cfg))
         bad["solver"]["boundary"]["channel"]["+y"] = {"type": "pressure"}
         gridgen.box_case(g, bad)
+
+
+def test_box_case_of_a_2d_reference_config():
+    """The reference's cavity config (walls on four sides of a unit box, level
+    4): its grid is the 16 x 16 box itself (the longest axis spans the root
+    cell), all fluid, every face a wall."""
+    cfg = dict(CONFIGS["cavity_small"])
+    cfg["solver"] = {"boundary": {"cube": {k: {"type": "wall", "model": "bounceback"} for k in ("-x", "+x", "-y", "+y")}}}
+    g = gridgen.grid_tables(cfg)
+    b = gridgen.box_case(g, cfg)
+    assert b["shape"] == (16, 16, 1)
+    assert (b["flags"] == gridgen.CELL_FLUID).all()
+    assert b["faces"][:4] == ("wall",) * 4
+    assert sorted(b["index"].tolist()) == list(range(256))
+
+
+def test_particle_config_errors_need_no_gpu():
+    from lbm_gb300.lpt import ParticleSolver
+
+    for bad in ({"dt": 1e-3, "gravity": [0, 1], "model": "gravityOnly"},
+                {"dt": 1e-3, "gravity": [0, 1], "integrationMethod": "RK4"},
+                {"gravity": [0, 1]}):
+        with pytest.raises(ConfigError):
+            ParticleSolver.from_config(bad, 2)
