@@ -157,6 +157,31 @@ def cpu_baseline(threads: int, budget_s: float = 12.0):
             "sample": f"D3Q19 sphere scaled to 128x64x64 (r=6), {steps} steps, FP64, OpenMP {threads} threads"}
 
 
+def mass_drift(tau, device, steps=100_000):
+    """Relative change of the FP64 mass sum over `steps` steps, per storage,
+    on a closed box: the sphere case scaled to 96 x 64 x 64 (radius 8),
+    periodic along x instead of inlet / outlet, free-slip sides, started from
+    a uniform flow u = 0.05 (bounce-back, periodic wrap and free slip all
+    conserve mass, so any change is rounding)."""
+    from lbm_gb300.solver import BoxSolver
+
+    shape = (96, 64, 64)
+    c = sphere_case(*shape, radius=8.0, center=(32.0, 32.0, 32.0))
+    flags = c["flags"].copy()
+    flags[flags > 1] = 0  # the inlet and outlet planes become fluid
+    out = {}
+    for st in ("f64", "f32", "f16dev", "bf16dev"):
+        s = BoxSolver(D3Q19, shape, 1.0 / tau, st, faces=("periodic", "periodic") + ("freeslip",) * 4, flags=flags,
+                      init_velocity=(0.05, 0.0, 0.0), device=device)
+        s.initial_condition()
+        m0 = s.mass_momentum()[0]
+        s.step(steps)
+        m1 = s.mass_momentum()[0]
+        s.close()
+        out[st] = float((m1 - m0) / m0)
+    return out
+
+
 def run_variant(storage, case, warmup, steps, device):
     from lbm_gb300.solver import BoxSolver
 
@@ -478,6 +503,12 @@ def main():
             del uu
     del u64
 
+    # mass conservation per storage (reported; a failure here never costs the line)
+    try:
+        drift = mass_drift(case["tau"], device)
+    except Exception as exc:
+        drift = {"error": str(exc)[:200]}
+
     # end to end through the C ABI with host buffers
     from lbm_gb300.solver import BoxSolver
 
@@ -529,7 +560,9 @@ def main():
                      "traffic": MEASURED_TRAFFIC_PER_STEP.get(args.storage), "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
                      "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},
-        "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + 2 * args.steps},
+        "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + 2 * args.steps,
+                     "mass_drift_per_1e5_steps": drift,
+                     "mass_drift_case": "closed D3Q19 sphere channel 96x64x64, periodic x, free-slip sides, u0 = 0.05"},
         "variants": variants,
         "gpu_launches": timed_launches,
         "e2e": e2e,
