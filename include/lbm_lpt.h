@@ -19,7 +19,9 @@
  * The step matches the reference bit for bit (IEEE doubles, the reference's
  * operation order, no contraction), except the Putnam drag factor's power
  * Re^(2/3) for 0.1 < Re <= 1000, which the reference takes from gcem and this
- * library from CUDA's pow.  Particle generation (injection) is not built.
+ * library from CUDA's pow.  Particle generation (injection) stays on the
+ * host, as in the reference; new particles enter through
+ * lbm_lpt_set_particles.
  *
  * Status codes are those of lbm_gpu.h; all calls are synchronous.
  */

@@ -45,7 +45,7 @@ def step(vars_: np.ndarray, ndim: int, model: int, implicit: bool, dt: float, gr
     D = ndim
     out = vars_.copy()
     R, RHO, DCI = 3 * D, 3 * D + 1, 3 * D + 4
-    for _ in range(nsteps):
+    for _ in range(nsteps if out.shape[0] else 0):
         rho_p0 = out[0, RHO]
         for p in range(out.shape[0]):
             row = out[p]

@@ -231,6 +231,8 @@ def run_lpt(name, cfg, steps):
 def write_lpt():
     for name, src, steps in LPT_CASES:
         run_lpt(name, load_config(src), steps)
+    # particle injection (3D): the reference's injection test, 100 steps
+    run_lpt("lpt_injection", load_config(("ref", "test/lpt/injection.json")), 100)
     for model, integration, dim in LPT_MODELS:
         run_lpt(f"lpt_{model}_{dim}d", lpt_model_config(model, integration, dim), 2000)
 

@@ -19,7 +19,7 @@ from lbm_gb300.lpt import ParticleSolver
 from lbm_gb300.solver import BoxSolver
 
 pytestmark = pytest.mark.gpu
-FIXTURES = caseio.list_lpt_fixtures()
+FIXTURES = [f for f in caseio.list_lpt_fixtures() if "injection" not in f]
 NLIN = {2, 5, 8}
 
 
