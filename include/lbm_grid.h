@@ -104,8 +104,10 @@ int lbm_grid_boundary(const lbm_grid* g, uint8_t* out);
 /* One surface of a "boundary" entry: for each direction in [dir_begin,
  * dir_end) and each boundary cell without a main neighbour in it that
  * object `obj` cuts, the pair (cell, direction) unless an earlier call took
- * it.  Appends up to `cap` pairs to cells / dirs, in the reference's order;
- * *n = number of pairs (LBM_ERR_INVALID if more than cap). */
+ * it.  *n = the number of pairs.  With cells and dirs NULL (and cap 0) the
+ * call only counts; otherwise it writes the pairs in the reference's order
+ * and takes them, or, when they are more than `cap`, returns
+ * LBM_ERR_INVALID and takes none. */
 int lbm_grid_add_surface(lbm_grid* g, int32_t obj, int32_t dir_begin, int32_t dir_end, int64_t* cells, int8_t* dirs, int64_t cap,
                          int64_t* n);
 /* Connect the cells of two periodic surfaces whose centres differ along

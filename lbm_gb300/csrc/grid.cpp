@@ -344,21 +344,28 @@ int lbm_grid_add_surface(lbm_grid* g, int32_t obj, int32_t dir_begin, int32_t di
   if(!g || !n || obj < 0 || obj >= static_cast<int>(g->objs.size())) return LBM_ERR_INVALID;
   const int D = g->D, M = 2 * D;
   if(dir_begin < 0 || dir_end > M || dir_begin >= dir_end) return LBM_ERR_INVALID;
+  // the pairs of this surface: a boundary cell without a main neighbour in
+  // the direction, cut by the object, and not taken by an earlier surface
+  // (within one call a pair cannot repeat, so counting needs no marks)
+  auto member = [&](int64_t c, int dir) {
+    return g->nbr[c * M + dir] == -1 && !(g->assigned[c] & (1u << dir)) && obj_cut(g->objs[obj], &g->centers[c * D], g->cell_length, D);
+  };
   int64_t count = 0;
   for(int dir = dir_begin; dir < dir_end; ++dir)
-    for(const int64_t c : g->bcells) {  // the boundary cells in cell order
-      if(g->nbr[c * M + dir] != -1) continue;
-      if(!obj_cut(g->objs[obj], &g->centers[c * D], g->cell_length, D)) continue;
-      if(g->assigned[c] & (1u << dir)) continue;  // taken by an earlier surface
-      g->assigned[c] = static_cast<uint8_t>(g->assigned[c] | (1u << dir));
-      if(count < cap && cells && dirs) {
-        cells[count] = c;
-        dirs[count]  = static_cast<int8_t>(dir);
-      }
-      ++count;
-    }
+    for(const int64_t c : g->bcells) count += member(c, dir) ? 1 : 0;
   *n = count;
-  return count <= cap ? LBM_OK : LBM_ERR_INVALID;
+  if(!cells || !dirs) return cap == 0 ? LBM_OK : LBM_ERR_INVALID;  // count only: nothing taken
+  if(count > cap) return LBM_ERR_INVALID;                          // nothing taken either
+  int64_t k = 0;
+  for(int dir = dir_begin; dir < dir_end; ++dir)
+    for(const int64_t c : g->bcells) {  // the boundary cells in cell order
+      if(!member(c, dir)) continue;
+      g->assigned[c] = static_cast<uint8_t>(g->assigned[c] | (1u << dir));
+      cells[k]       = c;
+      dirs[k]        = static_cast<int8_t>(dir);
+      ++k;
+    }
+  return LBM_OK;
 }
 
 int lbm_grid_connect_periodic(lbm_grid* g, const int64_t* cells_a, int64_t na, const int64_t* cells_b, int64_t nb) {

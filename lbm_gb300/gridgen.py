@@ -158,9 +158,6 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
         surfaces: Dict[str, dict] = {}
         periodic = {}
         boundary = config.get("solver", {}).get("boundary", {})
-        cap = n * 2 * ndim
-        cells = np.empty(cap, dtype=np.int64)
-        dirs = np.empty(cap, dtype=np.int8)
         for gname in sorted(boundary):
             entries = boundary[gname]
             for dname in sorted(entries):
@@ -173,11 +170,17 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
                 else:
                     raise ConfigError(f'boundary "{gname}": invalid direction "{dname}"')
                 got = C.c_int64()
+                m = 0
                 if gname in names:
-                    _lib.check(lib.lbm_grid_add_surface(h, names.index(gname), d0, d1, cells.ctypes.data, dirs.ctypes.data, cap,
-                                                        C.byref(got)), what="lbm_grid_add_surface")
-                m = int(got.value)
-                lst = cells[:m].copy()
+                    obj = names.index(gname)
+                    _lib.check(lib.lbm_grid_add_surface(h, obj, d0, d1, None, None, 0, C.byref(got)), what="lbm_grid_add_surface")
+                    m = int(got.value)
+                cells = np.empty(m, dtype=np.int64)
+                dirs = np.empty(m, dtype=np.int8)
+                if m:
+                    _lib.check(lib.lbm_grid_add_surface(h, obj, d0, d1, cells.ctypes.data, dirs.ctypes.data, m, C.byref(got)),
+                               what="lbm_grid_add_surface")
+                lst = cells
                 # Surface::addCell keeps one normal per cell: that of its last entry
                 last = {c: d for c, d in zip(lst.tolist(), dirs[:m].tolist())}
                 dl = np.array([last[c] for c in lst.tolist()], dtype=np.int64)

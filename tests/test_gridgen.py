@@ -195,3 +195,31 @@ def test_particle_config_errors_need_no_gpu():
                 {"gravity": [0, 1]}):
         with pytest.raises(ConfigError):
             ParticleSolver.from_config(bad, 2)
+
+
+def test_surface_call_takes_all_pairs_or_none():
+    """Counting takes nothing; a buffer too small is refused and takes
+    nothing either; a buffer of the counted size takes every pair once."""
+    import ctypes as C
+
+    from lbm_gb300._lib import LBM_OK
+
+    cfg = CONFIGS["cavity_small"]
+    lib = gridgen._grid_lib()
+    descs, names = gridgen.geometry_objects(cfg["geometry"], 2)
+    h = C.c_void_p()
+    assert lib.lbm_grid_create(2, 4, C.cast(descs, C.c_void_p), len(names), None, C.byref(h)) == LBM_OK
+    try:
+        n = C.c_int64()
+        assert lib.lbm_grid_add_surface(h, 0, 0, 4, None, None, 0, C.byref(n)) == LBM_OK
+        total = n.value
+        assert total == 4 * 16  # one row of 16 cells on each side of the box
+        cells = np.empty(total, dtype=np.int64)
+        dirs = np.empty(total, dtype=np.int8)
+        assert lib.lbm_grid_add_surface(h, 0, 0, 4, cells.ctypes.data, dirs.ctypes.data, total - 1, C.byref(n)) == -1
+        assert lib.lbm_grid_add_surface(h, 0, 0, 4, cells.ctypes.data, dirs.ctypes.data, total, C.byref(n)) == LBM_OK
+        assert n.value == total and sorted(set(zip(cells.tolist(), dirs.tolist()))) == sorted(zip(cells.tolist(), dirs.tolist()))
+        # now taken: a second surface over the same directions gets nothing
+        assert lib.lbm_grid_add_surface(h, 0, 0, 4, None, None, 0, C.byref(n)) == LBM_OK and n.value == 0
+    finally:
+        lib.lbm_grid_destroy(h)
