@@ -29,9 +29,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <new>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -63,6 +65,29 @@ uint64_t curve_index(const double* x, int D, int level) {
 int dir_axis(int dir) { return dir / 2; }
 int dir_sign(int dir) { return (dir & 1) ? 1 : -1; }
 
+// Run fn(begin, end, part) on `parts` contiguous slices of [0, n), one host
+// thread each.  Every slice writes only its own outputs, so the result does
+// not depend on the number of threads.
+// LBM_GRID_THREADS sets the number of slices (1-16) regardless of size.
+template <class F>
+void parallel_for(int64_t n, F fn, int* parts_out = nullptr) {
+  const int64_t min_per_thread = 1 << 16;
+  int           parts          = static_cast<int>(std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()), 16));
+  parts                        = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(parts, n / min_per_thread)));
+  if(const char* env = std::getenv("LBM_GRID_THREADS")) {
+    const long want = std::strtol(env, nullptr, 10);
+    if(want >= 1) parts = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({static_cast<int64_t>(want), 16, n})));
+  }
+  if(parts_out) *parts_out = parts;
+  if(parts == 1) {
+    fn(int64_t(0), n, 0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for(int t = 0; t < parts; ++t) pool.emplace_back(fn, n * t / parts, n * (t + 1) / parts, t);
+  for(auto& th : pool) th.join();
+}
+
 // Main neighbours (the adjacent positions that hold a cell) and the boundary
 // property (cut, and missing a main neighbour: determineBoundaryCells,
 // src/cartesiangrid.h:509-544) of the cells as they now stand.
@@ -74,21 +99,23 @@ void link_cells(lbm_grid& g) {
   for(int64_t c = 0; c < g.n; ++c) at[static_cast<size_t>(rel(c, 0) + nx * (rel(c, 1) + ny * rel(c, 2)))] = static_cast<int32_t>(c);
   const int64_t ext[3] = {nx, ny, nz};
   g.nbr.assign(g.n * M, -1);
-  for(int64_t c = 0; c < g.n; ++c)
-    for(int dir = 0; dir < M; ++dir) {
-      int64_t r[3] = {rel(c, 0), rel(c, 1), rel(c, 2)};
-      r[dir_axis(dir)] += dir_sign(dir);
-      if(r[dir_axis(dir)] < 0 || r[dir_axis(dir)] >= ext[dir_axis(dir)]) continue;
-      const int32_t m = at[static_cast<size_t>(r[0] + nx * (r[1] + ny * r[2]))];
-      if(m >= 0) g.nbr[c * M + dir] = m;
-    }
   g.bndry.assign(g.n, 0);
-  for(int64_t c = 0; c < g.n; ++c) {
-    if(!geom_cut(g, &g.centers[c * D], g.cell_length)) continue;
-    int present = 0;
-    for(int dir = 0; dir < M; ++dir) present += g.nbr[c * M + dir] != -1;
-    g.bndry[c] = present < M;
-  }
+  parallel_for(g.n, [&](int64_t c0, int64_t c1, int) {
+    for(int64_t c = c0; c < c1; ++c) {
+      int present = 0;
+      for(int dir = 0; dir < M; ++dir) {
+        int64_t r[3] = {rel(c, 0), rel(c, 1), rel(c, 2)};
+        r[dir_axis(dir)] += dir_sign(dir);
+        if(r[dir_axis(dir)] < 0 || r[dir_axis(dir)] >= ext[dir_axis(dir)]) continue;
+        const int32_t m = at[static_cast<size_t>(r[0] + nx * (r[1] + ny * r[2]))];
+        if(m >= 0) {
+          g.nbr[c * M + dir] = m;
+          ++present;
+        }
+      }
+      g.bndry[c] = present < M && geom_cut(g, &g.centers[c * D], g.cell_length);
+    }
+  });
   list_boundary_cells(g);
 }
 
@@ -203,26 +230,49 @@ int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int3
     uint64_t key;
     int32_t  p[3];
   };
-  std::vector<Kept> kept;
-  const int64_t     nx = g->ext[0], ny = g->ext[1], nz = g->ext[2];
-  for(int64_t k = 0; k < nz; ++k)
-    for(int64_t j = 0; j < ny; ++j)
-      for(int64_t i = 0; i < nx; ++i) {
-        const int64_t p[3] = {g->lo[0] + i, D > 1 ? g->lo[1] + j : 0, D > 2 ? g->lo[2] + k : 0};
-        double        c[3];
-        for(int d = 0; d < D; ++d) c[d] = g->cv[d][p[d]];
-        if(!(geom_cut(*g, c, g->cell_length) || geom_inside(*g, c))) continue;
-        // curve index of the centre in the unit cube of the root cell
-        // (reorderHilbertCurve, cartesiangrid_generation.h:677-680)
-        double x[3];
-        for(int d = 0; d < D; ++d) x[d] = ((c[d] - g->cog[d]) + 0.5 * g->len0) / g->len0;
-        kept.push_back({curve_index(x, D, level), {static_cast<int32_t>(p[0]), static_cast<int32_t>(p[1]), static_cast<int32_t>(p[2])}});
-      }
+  const int64_t nx = g->ext[0], ny = g->ext[1], nz = g->ext[2];
+  // every slice of the candidate positions collects and sorts its own kept
+  // cells; the sorted slices are then merged (the keys are distinct, so the
+  // order does not depend on the slicing)
+  std::vector<std::vector<Kept>> part(16);
+  int                            parts = 1;
+  const auto                     by_key = [](const Kept& a, const Kept& b) { return a.key < b.key; };
+  parallel_for(
+      nx * ny * nz,
+      [&](int64_t q0, int64_t q1, int t) {
+        std::vector<Kept>& kept = part[t];
+        for(int64_t q = q0; q < q1; ++q) {
+          const int64_t i = q % nx, j = (q / nx) % ny, k = q / (nx * ny);
+          const int64_t p[3] = {g->lo[0] + i, D > 1 ? g->lo[1] + j : 0, D > 2 ? g->lo[2] + k : 0};
+          double        c[3];
+          for(int d = 0; d < D; ++d) c[d] = g->cv[d][p[d]];
+          if(!(geom_cut(*g, c, g->cell_length) || geom_inside(*g, c))) continue;
+          // curve index of the centre in the unit cube of the root cell
+          // (reorderHilbertCurve, cartesiangrid_generation.h:677-680)
+          double x[3];
+          for(int d = 0; d < D; ++d) x[d] = ((c[d] - g->cog[d]) + 0.5 * g->len0) / g->len0;
+          kept.push_back({curve_index(x, D, level), {static_cast<int32_t>(p[0]), static_cast<int32_t>(p[1]), static_cast<int32_t>(p[2])}});
+        }
+        std::sort(kept.begin(), kept.end(), by_key);
+      },
+      &parts);
+  // pairwise merges of neighbouring slices until one is left
+  for(int width = 1; width < parts; width *= 2) {
+    std::vector<std::thread> pool;
+    for(int a = 0; a + width < parts; a += 2 * width)
+      pool.emplace_back([&, a, width]() {
+        std::vector<Kept> merged(part[a].size() + part[a + width].size());
+        std::merge(part[a].begin(), part[a].end(), part[a + width].begin(), part[a + width].end(), merged.begin(), by_key);
+        part[a].swap(merged);
+        std::vector<Kept>().swap(part[a + width]);
+      });
+    for(auto& th : pool) th.join();
+  }
+  std::vector<Kept>& kept = part[0];
   if(kept.empty() || kept.size() >= (size_t(1) << 31)) {
     delete g;
     return LBM_ERR_INVALID;
   }
-  std::sort(kept.begin(), kept.end(), [](const Kept& a, const Kept& b) { return a.key < b.key; });
   for(size_t i = 1; i < kept.size(); ++i)
     if(kept[i].key == kept[i - 1].key) {  // the reference stops on duplicated curve ids
       delete g;
@@ -452,7 +502,8 @@ int lbm_grid_neighbors(const lbm_grid* g, int64_t* out) {
   static constexpr int e2[4][2]  = {{1, 1}, {1, -1}, {-1, -1}, {-1, 1}};
   static constexpr int e3[12][3] = {{-1, -1, 0}, {-1, 1, 0}, {1, -1, 0}, {1, 1, 0},  {-1, 0, -1}, {-1, 0, 1},
                                     {1, 0, -1},  {1, 0, 1},  {0, -1, -1}, {0, -1, 1}, {0, 1, -1},  {0, 1, 1}};
-  for(int64_t c = 0; c < g->n; ++c) {
+  parallel_for(g->n, [&](int64_t c0, int64_t c1, int) {
+  for(int64_t c = c0; c < c1; ++c) {
     int64_t* o = out + c * W;
     for(int dir = 0; dir < M; ++dir) o[dir] = g->nbr[c * M + dir];
     if(D == 2)
@@ -468,6 +519,7 @@ int lbm_grid_neighbors(const lbm_grid* g, int64_t* out) {
         o[M + e] = step(step(c, ax[0], sg[0]), ax[1], sg[1]);
       }
   }
+  });
   return LBM_OK;
 }
 

@@ -223,3 +223,18 @@ def test_surface_call_takes_all_pairs_or_none():
         assert lib.lbm_grid_add_surface(h, 0, 0, 4, None, None, 0, C.byref(n)) == LBM_OK and n.value == 0
     finally:
         lib.lbm_grid_destroy(h)
+
+
+@pytest.mark.parametrize("threads", ["1", "3", "8"])
+def test_host_build_is_independent_of_the_thread_count(threads, monkeypatch):
+    """The host build splits positions, cells and neighbour rows over threads
+    (LBM_GRID_THREADS forces the split): the tables must not change."""
+    cfg = channel_sphere_config(level=6, radius=5.5)
+    monkeypatch.setenv("LBM_GRID_THREADS", "1")
+    one = gridgen.grid_tables(cfg)
+    monkeypatch.setenv("LBM_GRID_THREADS", threads)
+    many = gridgen.grid_tables(cfg)
+    assert np.array_equal(one.centers, many.centers)
+    assert np.array_equal(one.nghbr, many.nghbr)
+    for k in one.surfaces:
+        assert np.array_equal(one.surfaces[k]["cells"], many.surfaces[k]["cells"])
