@@ -48,3 +48,23 @@ def test_single_process_needs_no_process_group():
     import bench
 
     assert bench.job_throughput(50.0, 2000, 5, None, "cpu") == (50.0, pytest.approx(2000 * 5 / 0.05 / 1e6))
+
+
+def test_reference_arm_prints_its_line(monkeypatch, capsys):
+    """`bench.py --impl reference` runs on the host alone: one JSON line with
+    the keys the reference arm needs (a shortened CPU sample here)."""
+    import json
+    import sys
+
+    import bench
+
+    real = bench.cpu_baseline
+    monkeypatch.setattr(bench, "cpu_baseline", lambda threads: real(min(threads, 2), budget_s=0.2))
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1"])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "MLUPS" and line["value"] > 0
+    assert line["higher_is_better"] is True
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
