@@ -42,9 +42,9 @@ D3Q19 = 4
 B_PER_CELL = {"f64": 2 * 19 * 8 + 1, "f32": 2 * 19 * 4 + 1, "f16dev": 2 * 19 * 2 + 1, "bf16dev": 2 * 19 * 2 + 1}
 METRIC = "MLUPS (D3Q19 sphere 512x256x256, FP16-deviation storage)"
 # DRAM bytes (read + write) per step of this workload, averaged over the two
-# step parities (bulk + boundary + outlet kernels), from the one-pass ncu
-# launch list recorded in profiles/launches_bench_d3q19_sphere_512x256x256.md
-MEASURED_TRAFFIC_PER_STEP = {"f16dev": 2.58e9}
+# step parities (bulk + boundary + outlet kernels): taken from an ncu capture
+# of this workload's step kernels, not measured by this script
+PROFILED_TRAFFIC_PER_STEP = {"f16dev": 2.58e9}
 
 
 def peaks():
@@ -407,7 +407,8 @@ def main():
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
                     help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
-    ap.add_argument("--kernel", default=None, choices=["thread", "staged", "paired"], help="--profile-case: force this bulk kernel")
+    ap.add_argument("--kernel", default=None, choices=["thread", "staged", "paired", "rows"],
+                    help="--profile-case: force this bulk kernel")
     args = ap.parse_args()
     if args.profile_case:
         from lbm_gb300.solver import BoxSolver
@@ -557,7 +558,9 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU", "threads_per_block": tpb,
                    "bulk_kernel": bulk_kernel},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": MEASURED_TRAFFIC_PER_STEP.get(args.storage), "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
+                     "traffic": PROFILED_TRAFFIC_PER_STEP.get(args.storage),
+                     "traffic_source": "ncu capture of this workload's step kernels (dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "per step), recorded with the source; not measured in this run", "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
                      "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},
         "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + 2 * args.steps,

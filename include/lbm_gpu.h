@@ -7,7 +7,7 @@
  * and the boundary conditions are LBMBndInterface objects driven through
  * std::function accessors (src/lbm/bnd/bnd_interface.h:7-24).  The entry
  * points below replace those, one for one, and are what a GPU branch inside
- * LBMSolver::run() calls (see INTEGRATION.md for the binding):
+ * LBMSolver::run() calls:
  *
  *   lbm_gpu_create            <- LBMSolver::transferGrid + loadConfiguration
  *                                (src/lbm/solver.cpp:758-801, :70-163)
@@ -143,16 +143,19 @@ void        lbm_gpu_destroy(lbm_gpu_ctx* ctx);
  * belongs to another allocator (a framework's caching allocator, a fixed
  * arena) and latency-critical code that cannot afford cudaMalloc's implicit
  * synchronisation.  It computes out[v] = sum_i |vars[v*ncells+i] -
- * varsold[v*ncells+i]| for v < nvar (the reference's sumAbsDiff,
- * src/lbm/solver.cpp:808-815) on caller-owned DEVICE arrays, variable-major,
- * writing nvar doubles to the DEVICE array `out`, asynchronously on `stream`
- * (a cudaStream_t; NULL = legacy default stream) of the current device.
+ * varsold[v*ncells+i]| for v < nvar, the convergence residual of
+ * lbm_gpu_residual, on caller-owned DEVICE arrays, variable-major, writing
+ * nvar doubles to the DEVICE array `out`, asynchronously on `stream` (a
+ * cudaStream_t; NULL = legacy default stream) of the current device.
  * Scratch: a fixed array in the library's device image (304 x
  * LBM_GPU_NOALLOC_MAX_VARS doubles per GPU, kept until the process exits),
  * shared by every call: calls that overlap on the GPU race.  nvar above
  * LBM_GPU_NOALLOC_MAX_VARS is rejected with LBM_ERR_INVALID.  The first call
  * on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture. */
+ * make that first call before any stream capture (a first call inside a
+ * capture returns LBM_ERR_INVALID).  Calls outside capture look the address
+ * up again, so the entry point stays valid across a device reset; a call
+ * inside a capture uses the address of the last call outside one. */
 #define LBM_GPU_NOALLOC_MAX_VARS 8
 int lbm_gpu_residual_noalloc(const double* vars, const double* varsold, int64_t ncells, int32_t nvar, double* out, void* stream);
 

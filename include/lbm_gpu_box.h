@@ -97,19 +97,38 @@ int lbm_gpu_box_probe(lbm_gpu_ctx* ctx, const int64_t* cells, int64_t n, double*
 int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block);
 /* Bulk step kernel of a box context: LBM_BOX_KERNEL_THREAD (one cell per
  * thread, one global load per population), LBM_BOX_KERNEL_STAGED (each CTA
- * stages whole rows in shared memory with bulk copies) or
- * LBM_BOX_KERNEL_PAIRED (two x-adjacent cells per thread, 2-element loads and
- * stores where aligned); lbm_gpu_create_box picks the fastest by timing them.
- * All give bit-identical results.  kernel < 0 only queries.
- * LBM_ERR_UNSUPPORTED when the box does not qualify: staging needs nx times
- * the storage size to be a multiple of 16 bytes; pairing needs nx even and a
+ * stages row segments in shared memory with bulk copies and stores straight
+ * to global memory), LBM_BOX_KERNEL_PAIRED (two x-adjacent cells per thread,
+ * 2-element loads and stores where aligned) or LBM_BOX_KERNEL_ROWS (each
+ * stage holds one whole x-row; bulk copies load it and store it back, the
+ * cells update it in place in shared memory); lbm_gpu_create_box picks the
+ * fastest by timing them.  All give bit-identical results.  kernel < 0 only
+ * queries.  LBM_ERR_UNSUPPORTED when the box does not qualify: staging needs
+ * nx times the storage size to be a multiple of 16 bytes (row staging also
+ * nx <= 1024 and, for FP64 D3Q19, nx <= 512); pairing needs nx even and a
  * 32- or 16-bit storage. */
-typedef enum lbm_box_kernel { LBM_BOX_KERNEL_THREAD = 0, LBM_BOX_KERNEL_STAGED = 1, LBM_BOX_KERNEL_PAIRED = 2 } lbm_box_kernel;
+typedef enum lbm_box_kernel {
+  LBM_BOX_KERNEL_THREAD = 0,
+  LBM_BOX_KERNEL_STAGED = 1,
+  LBM_BOX_KERNEL_PAIRED = 2,
+  LBM_BOX_KERNEL_ROWS   = 3
+} lbm_box_kernel;
 int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected);
 /* The autotuner times even (local) and odd (streaming) steps separately and
  * may pick a different kernel for each: the kernels of both parities
  * (lbm_gpu_box_select_kernel sets both, and reports -1 when they differ). */
 int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd);
+
+/* TEST ONLY.  The staged kernels' (LBM_BOX_KERNEL_STAGED and
+ * LBM_BOX_KERNEL_ROWS) pipeline waits are bounded (0.5 s each);
+ * when one runs out the kernel records a flag, lets its copies in flight
+ * land and returns, and the step call reports LBM_ERR_TIMEOUT (the state of
+ * that step is invalid; re-initialise or reload it).  This sets the limit of
+ * each wait (1 ns .. 0.5 s) and, with starve = 1, makes every CTA leave its
+ * first segment unarmed, so the waits on it run out: a device-side timeout
+ * without a fault.  starve = 0 and limit 500000000 restore the defaults.  No
+ * counterpart in the reference, which has no device waits. */
+int lbm_gpu_box_test_wait(lbm_gpu_ctx* ctx, int64_t limit_ns, int32_t starve);
 
 /* Run nsteps exactly as lbm_gpu_step does (captured per-parity graphs, the
  * last two steps recording the residual) with one CUDA event pair around the

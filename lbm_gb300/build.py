@@ -29,6 +29,7 @@ UNITS = {
     "reduce.cu": [],
     "box.cu": [],
     "box_tma.cu": [],
+    "box_rows.cu": [],
     "capi.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],

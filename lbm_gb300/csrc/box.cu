@@ -769,6 +769,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   const int      kind   = odd ? b->kind_odd : b->kind_even;
   const bool     staged = kind == LBM_BOX_KERNEL_STAGED;
   const bool     paired = kind == LBM_BOX_KERNEL_PAIRED && mom == 0;  // residual steps use the per-thread kernel
+  const bool     rows   = kind == LBM_BOX_KERNEL_ROWS && mom == 0;    // like the per-thread kernel: XFACE cells in line
   // the per-thread odd kernel steps the XFACE cells itself; with the others the
   // boundary kernel takes them too (they close its list)
   // and its SFACE cells are taken by the boundary kernel's face blocks
@@ -786,8 +787,13 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     const cudaError_t e = box_tma_bulk(b, odd, mom, s, &nbulk);
     if(e != cudaSuccess) return e;
   }
+  if(rows) {
+    // before the boundary kernel, whose cells' slots it writes back unchanged
+    const cudaError_t e = box_rows_bulk(b, odd, s);
+    if(e != cudaSuccess) return e;
+  }
   if(odd) {
-    if(staged) {
+    if(staged || rows) {
     } else if(paired) {
       if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, true><<<gp, tpb, 0, s>>>(b->p);
     } else if(mom == 0) {
@@ -803,7 +809,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     }
     if(mom == 2) b->res_slots = nbulk + static_cast<int64_t>(nbb) * 4;
   } else {
-    if(staged) {
+    if(staged || rows) {
     } else if(paired) {
       if constexpr(ST != LBM_STORE_F64) k_box_pair<LAT, EQ, ST, false><<<gp, tpb, 0, s>>>(b->p);
     } else if(mom == 0) {
@@ -885,14 +891,15 @@ int cerr(std::string& err, cudaError_t e, const char* what) {
 
 // a staged kernel that gave up waiting for its copies leaves a flag behind
 int check_wait_flag(BoxState* b, std::string& err) {
-  if(b->kind_even != LBM_BOX_KERNEL_STAGED && b->kind_odd != LBM_BOX_KERNEL_STAGED) return LBM_OK;
+  const auto waits = [](int k) { return k == LBM_BOX_KERNEL_STAGED || k == LBM_BOX_KERNEL_ROWS; };
+  if(!waits(b->kind_even) && !waits(b->kind_odd)) return LBM_OK;
   int         flag = 0;
   cudaError_t e    = cudaMemcpy(&flag, b->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if(e != cudaSuccess) return cerr(err, e, "wait flag");
   if(flag) {
     cudaMemset(b->d_err, 0, sizeof(int));
     err = "staged step kernel: a bulk-copy wait timed out (state of this step is invalid)";
-    return LBM_ERR_CUDA;
+    return LBM_ERR_TIMEOUT;
   }
   return LBM_OK;
 }
@@ -901,6 +908,7 @@ bool box_kernel_supported(const BoxState* b, int kind) {
   if(kind == LBM_BOX_KERNEL_THREAD) return true;
   if(kind == LBM_BOX_KERNEL_STAGED) return box_tma_supported(b);
   if(kind == LBM_BOX_KERNEL_PAIRED) return b->p.nx % 2 == 0 && b->desc.storage != LBM_STORE_F64;
+  if(kind == LBM_BOX_KERNEL_ROWS) return box_rows_supported(b);
   return false;
 }
 
@@ -1397,7 +1405,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
     // (local) and odd (streaming) steps may each take a different one
     float best_even = 1e30f, best_odd = 1e30f;
     int   pick_even = LBM_BOX_KERNEL_THREAD, pick_odd = LBM_BOX_KERNEL_THREAD;
-    for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED}) {
+    for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED, LBM_BOX_KERNEL_ROWS}) {
       if(!box_kernel_supported(b, kind)) continue;
       b->kind_even = b->kind_odd = kind;
       float       ev = 0, od = 0;
@@ -1420,7 +1428,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
     if(pick_even != pick_odd) {
       float best_pair = 1e30f;
       int   pe = pick_even, po = pick_odd;
-      for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED}) {
+      for(int kind : {LBM_BOX_KERNEL_THREAD, LBM_BOX_KERNEL_STAGED, LBM_BOX_KERNEL_PAIRED, LBM_BOX_KERNEL_ROWS}) {
         if(!box_kernel_supported(b, kind)) continue;
         b->kind_even = b->kind_odd = kind;
         const float ms = time_pair(b, b->tuned_tpb, stream);
@@ -1599,10 +1607,12 @@ int lbm_gpu_box_autotune(lbm_gpu_ctx* ctx, int32_t* threads_per_block) {
 
 int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selected) {
   BoxState* b = lbm_internal_box(ctx);
-  if(!b || kernel > LBM_BOX_KERNEL_PAIRED) return LBM_ERR_INVALID;
+  if(!b || kernel > LBM_BOX_KERNEL_ROWS) return LBM_ERR_INVALID;
   if(kernel >= 0 && !box_kernel_supported(b, kernel)) {
     lbm_internal_set_error(ctx, kernel == LBM_BOX_KERNEL_STAGED ? "box does not qualify for the staged kernel (rows must be 16-byte multiples)"
-                                                               : "box does not qualify for the paired kernel (nx even, FP32/FP16/BF16 storage)");
+                                : kernel == LBM_BOX_KERNEL_ROWS ? "box does not qualify for the row-staged kernel (rows of 16-byte multiples, "
+                                                                  "at most 1024 cells, stages within shared memory)"
+                                                                : "box does not qualify for the paired kernel (nx even, FP32/FP16/BF16 storage)");
     return LBM_ERR_UNSUPPORTED;
   }
   if(kernel >= 0 && (kernel != b->kind_even || kernel != b->kind_odd)) {
@@ -1611,6 +1621,16 @@ int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selecte
     b->kind_even = b->kind_odd = kernel;
   }
   if(selected) *selected = b->kind_even == b->kind_odd ? b->kind_even : -1;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_test_wait(lbm_gpu_ctx* ctx, int64_t limit_ns, int32_t starve) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b || limit_ns <= 0 || limit_ns > 500000000 || (starve != 0 && starve != 1)) return LBM_ERR_INVALID;
+  cudaStreamSynchronize(lbm_internal_stream(ctx));
+  drop_graphs(b);  // the graphs hold the old launch parameters
+  b->wait_limit_ns = static_cast<uint64_t>(limit_ns);
+  b->wait_starve   = starve;
   return LBM_OK;
 }
 

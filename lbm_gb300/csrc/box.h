@@ -80,6 +80,11 @@ struct BoxState {
   int          kind_even = 0;        // lbm_box_kernel of the even steps: per-thread, staged (box_tma.cu) or paired
   int          kind_odd  = 0;        // and of the odd steps
   int*         d_err     = nullptr;  // set by a staged kernel whose bounded wait ran out
+  // bounded waits of the staged kernel: the limit of each wait, and the
+  // test-only starvation switch (the first segment of every CTA is never
+  // armed, so its wait runs out); see lbm_gpu_box_test_wait
+  uint64_t     wait_limit_ns = 500000000ull;
+  int          wait_starve   = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one-step graphs for even and odd parity
 };
 
@@ -95,6 +100,11 @@ void        box_destroy(BoxState* b);
 // the launch; *slots = residual partial slots the launch writes
 bool        box_tma_supported(const BoxState* b);
 cudaError_t box_tma_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots);
+// row-staged bulk kernel (box_rows.cu), plain steps only: whether the box
+// qualifies, and the launch.  Its odd step must run before the boundary
+// kernel: it writes back the unchanged slots of the cells it does not step.
+bool        box_rows_supported(const BoxState* b);
+cudaError_t box_rows_bulk(BoxState* b, bool odd, cudaStream_t s);
 
 }  // namespace lbm
 

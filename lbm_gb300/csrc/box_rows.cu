@@ -1,0 +1,389 @@
+// Dense-box step with whole x-rows staged in shared memory and moved by bulk
+// copies (TMA) in both directions.
+//
+// The per-thread step kernel (box.cu) issues one 2-byte global load and one
+// 2-byte global store per population (FP16 storage), each with its own 64-bit
+// address arithmetic: about 410 warp instructions per 32 cells, so it is bound
+// by instruction issue and memory latency together.  Here one elected thread
+// moves every row of the step with 1D bulk copies and the cell threads touch
+// shared memory only, at compile-time offsets from one base per cell.
+//
+// One pipeline stage holds one x-row (y, z) of the step: per plane p a staged
+// row of WR elements, the row's values at positions [0, nx) sitting at index
+// H..H+nx-1 (H = one 16-byte vector of halo on either side).
+//   even step: plane p, row (y, z).  Cell x reads f_q at [q][x] and writes its
+//              post-collision f_q to [opp q][x] -- the AA even step, in place.
+//   odd step:  plane p, row (y + c_py, z + c_pz), positions [-H, nx + H).  Cell
+//              x pulls f_q = A[opp q][x - c_q], which is staged at
+//              [opp q][x - c_qx], and pushes its post-collision f_q to
+//              A[q][x + c_q], staged at [q][x + c_qx].  That slot is the one
+//              the cell pulled f_{opp q} from: every staged slot is read and
+//              then written by the one thread that owns it, so the update is
+//              in place here too.
+// After the row's cells, every plane's [0, nx) goes back to the same global
+// row with one bulk store.  A cell the kernel does not step (a solid, a cell
+// whose links the boundary kernel resolves) leaves its staged slots as they
+// were loaded, so the store writes back unchanged values there.  The slots a
+// row's store covers belong to that row's cells or to no cell at all: position
+// 0 of a c_px = +1 plane and position nx-1 of a c_px = -1 plane receive
+// nothing through an open face, and with periodic or wall x faces they belong
+// to the row's own end cell, which the boundary kernel steps after this
+// kernel.  Pushes through the row ends (the inlet's c_x < 0 populations, the
+// outlet's c_x > 0 ones) land in the halo, which is never stored.
+//
+// The odd step covers the interior rows (the face rows hold only cells the
+// boundary kernel steps); within them it steps what the per-thread odd step
+// steps: fluid cells with no link to resolve, and the inlet / outlet face cells
+// (XFACE) in line.  Results are bitwise those of the per-thread kernel: the
+// same loads, collision and stores per cell.
+//
+// Pipeline per CTA: warp 0 lane 0 keeps stages of row loads in flight (full
+// barriers); eight consumer warps step the row in shared memory, fence it for
+// the async proxy and meet at a named barrier; consumer thread 0 then issues
+// the row's bulk stores, and once the previous row's stores have read their
+// stage it releases that stage (empty barrier).  Every mbarrier wait is
+// bounded; a timed-out wait sets the error flag, the consumers agree on it at
+// the named barrier and leave together after thread 0's stores completed, and
+// the producer lets its own loads land before it leaves.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "box.h"
+#include "box_device.cuh"
+#include "bulk_copy.cuh"
+#include "lattice.cuh"
+#include "step_common.cuh"
+
+namespace lbm {
+namespace {
+
+constexpr int kRowWarps   = 8;               // consumer warps per CTA
+constexpr int kRowThreads = 32 * kRowWarps;  // consumer threads
+
+// halo elements on either side of a staged row: one 16-byte vector
+template <class T>
+constexpr int row_halo() {
+  return static_cast<int>(16 / sizeof(T));
+}
+// pipeline stages per CTA
+template <class T>
+constexpr int row_stages() {
+  return sizeof(T) <= 2 ? 3 : 2;
+}
+// staged row width (elements) for rows of up to 256*K cells
+template <class T, int K>
+constexpr int row_width() {
+  return 256 * K + 2 * row_halo<T>();
+}
+template <int LAT, class T, int K>
+constexpr size_t row_smem() {
+  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 2 * row_stages<T>();
+}
+constexpr size_t kRowSmemMax = 200 * 1024;
+
+struct RowList {
+  FastDiv  nrows;     // rows per z-slab in the list
+  int      y0, z0;    // first row: y in [y0, y0 + nrows), z from z0
+  int      count;     // rows in the list
+  int*     err;       // set to 1 when a wait times out
+  uint64_t limit_ns;  // limit of each pipeline wait
+  int      starve;    // test only: the producer never arms the CTA's first row, so the waits on it run out
+};
+
+// One cell of a staged row.  bx: the cell's element in plane 0 of the stage
+// (index H + x).
+template <int LAT, int EQ, int ST, bool ODD, int WR>
+__device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z) {
+  using L         = Lattice<LAT>;
+  using S         = Store<ST>;
+  using T         = typename S::T;
+  using C         = typename S::C;
+  constexpr int Q = L::Q;
+  const int     cell = x + P.nx * (y + P.ny * z);
+  const uint8_t flag = P.flags[cell];
+  const uint8_t type = flag & TYPE_MASK;
+  bool          work, special;
+  if constexpr(ODD) {
+    const bool xf = (flag & XFACE) != 0;
+    work          = flag == LBM_CELL_FLUID || xf;  // fluid and not LINKED, or an inlet / outlet face cell
+    special       = xf;
+  } else {
+    work    = type != LBM_CELL_SOLID;
+    special = type != LBM_CELL_FLUID;
+  }
+  if(!work) return;
+  // one vote per warp: warps of plain fluid cells take the path without the
+  // inlet / outlet / Dirichlet branches
+  const bool any_special = __any_sync(__activemask(), special);
+  C          f[Q];
+  if(!any_special) {
+    static_for<Q>([&](auto qc) {
+      constexpr int q = decltype(qc)::value;
+      if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
+      else f[q] = S::load(bx[q * WR]);
+    });
+    collide<LAT, EQ, C>(P, f, nullptr);
+  } else {
+    const bool emit = ODD ? (special && type == LBM_CELL_INLET) : (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
+    if(emit) {
+      emit_equilibrium<LAT, EQ, C>(P, f, cell);
+    } else {
+      static_for<Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
+        else f[q] = S::load(bx[q * WR]);
+      });
+      if(type == LBM_CELL_OUTLET) {
+        // links from beyond +x: what the upstream cell received (ghost plane)
+        const T*  A  = static_cast<const T*>(P.pop);
+        const int NA = static_cast<int>(P.nalloc);
+        static_for<Q>([&](auto qc) {
+          constexpr int q = decltype(qc)::value;
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+        });
+      }
+      collide<LAT, EQ, C>(P, f, nullptr);
+    }
+  }
+  static_for<Q>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    if constexpr(ODD) bx[q * WR + L::c(q, 0)] = S::store(f[q]);
+    else bx[L::opp(q) * WR] = S::store(f[q]);
+  });
+}
+
+// resident CTAs per SM the register budget aims at (what the stages of shared
+// memory allow)
+template <int ST>
+constexpr int row_min_ctas() {
+  return ST == LBM_STORE_F64 ? 1 : (ST == LBM_STORE_F32 ? 2 : 3);
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int K>
+__global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_rows(BoxParams P, RowList R) {
+  using L             = Lattice<LAT>;
+  using S             = Store<ST>;
+  using T             = typename S::T;
+  constexpr int Q     = L::Q;
+  constexpr int H     = row_halo<T>();
+  constexpr int NST   = row_stages<T>();
+  constexpr int WR    = row_width<T, K>();
+  constexpr int STAGE = Q * WR;  // staged elements per row
+  extern __shared__ __align__(128) unsigned char smem[];
+  T*        buf   = reinterpret_cast<T*>(smem);
+  uint64_t* full  = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);
+  uint64_t* empty = full + NST;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G    = static_cast<int>(gridDim.x);
+  // each CTA takes one contiguous run of rows
+  const int per   = (R.count + G - 1) / G;
+  const int first = static_cast<int>(blockIdx.x) * per;
+  const int nloc  = first < R.count ? min(per, R.count - first) : 0;
+  if(threadIdx.x == 0) {
+#pragma unroll
+    for(int s = 0; s < NST; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+
+  T* const  A  = static_cast<T*>(P.pop);
+  const int NA = static_cast<int>(P.nalloc);
+  const int nx = P.nx, ny = P.ny;
+  auto      coords = [&](int i, int& y, int& z) {
+    const uint32_t r  = static_cast<uint32_t>(first + i);
+    const uint32_t zz = fdiv(r, R.nrows);
+    y                 = R.y0 + static_cast<int>(r - zz * R.nrows.d);
+    z                 = R.z0 + static_cast<int>(zz);
+  };
+
+  if(warp == 0) {
+    // ---- producer ----
+    if(lane == 0) {
+      const uint32_t bytes  = static_cast<uint32_t>((ODD ? nx + 2 * H : nx) * sizeof(T));
+      int            issued = 0;  // rows [0, issued) are armed (all but a starved one)
+      for(int i = 0; i < nloc; ++i) {
+        const int st = i % NST;
+        if(i >= NST && !mbar_wait_bounded(smem_u32(&empty[st]), static_cast<uint32_t>((i / NST - 1) & 1), R.limit_ns)) {
+          atomicExch(R.err, 1);
+          break;
+        }
+        issued = i + 1;
+        if(R.starve && i == 0) continue;  // test only: nothing arms full[0], its waits run out
+        int y, z;
+        coords(i, y, z);
+        const uint32_t b = smem_u32(&full[st]);
+        mbar_expect_tx(b, bytes * Q);
+        T* const dst0 = buf + st * STAGE + (ODD ? 0 : H);
+        static_for<Q>([&](auto qc) {
+          constexpr int p  = decltype(qc)::value;
+          const int     ys = ODD ? y + L::c(p, 1) : y;
+          const int     zs = ODD ? z + L::c(p, 2) : z;
+          const T*      src = A + p * NA + nx * (ys + ny * zs) - (ODD ? H : 0);
+          bulk_g2s(smem_u32(dst0 + p * WR), src, bytes, b);
+        });
+      }
+      // every load this CTA issued has landed before its threads can all exit
+      for(int j = issued > NST ? issued - NST : 0; j < issued; ++j)
+        if(!(R.starve && j == 0))
+          mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1), kDrainLimitNs);
+    }
+    return;
+  }
+
+  // ---- consumers ----
+  const int tid = threadIdx.x - 32;
+  for(int i = 0; i < nloc; ++i) {
+    const int st = i % NST;
+    int       y, z;
+    coords(i, y, z);
+    const bool got = mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns);
+    if(!consumers_all(got, kRowThreads)) {  // every consumer leaves, or none
+      if(tid == 0) {
+        atomicExch(R.err, 1);
+        bulk_wait_all();  // the stores already issued complete before the CTA exits
+      }
+      return;
+    }
+    T* const stage = buf + st * STAGE + H;
+#pragma unroll 1
+    for(int x = tid; x < nx; x += kRowThreads) row_cell<LAT, EQ, ST, ODD, WR>(P, stage + x, x, y, z);
+    fence_async_smem();  // this thread's writes are visible to the bulk stores
+    consumers_sync(kRowThreads);
+    if(tid == 0) {
+      const uint32_t bytes = static_cast<uint32_t>(nx * sizeof(T));
+      static_for<Q>([&](auto qc) {
+        constexpr int p  = decltype(qc)::value;
+        const int     ys = ODD ? y + L::c(p, 1) : y;
+        const int     zs = ODD ? z + L::c(p, 2) : z;
+        bulk_s2g(A + p * NA + nx * (ys + ny * zs), smem_u32(stage + p * WR), bytes);
+      });
+      bulk_commit();
+      bulk_wait_read<1>();  // the previous row's stores have read their stage: release it
+      if(i > 0) mbar_arrive(smem_u32(&empty[(i - 1) % NST]));
+    }
+  }
+  if(tid == 0) bulk_wait_all();
+}
+
+template <int LAT, int EQ, int ST, bool ODD, int K>
+cudaError_t launch_rows_one(BoxState* b, const RowList& R, cudaStream_t s) {
+  using T           = typename Store<ST>::T;
+  constexpr size_t smem = row_smem<LAT, T, K>();
+  if constexpr(smem > kRowSmemMax) {
+    return cudaErrorInvalidValue;
+  } else {
+    auto kern = k_box_rows<LAT, EQ, ST, ODD, K>;
+    // resident CTAs on the whole GPU, worked out once per instantiation
+    static int resident = 0;
+    if(resident == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      if(e != cudaSuccess) return e;
+      int per_sm = 0;
+      e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRowThreads + 32, smem);
+      if(e != cudaSuccess) return e;
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      resident = std::max(per_sm, 1) * sms;
+    }
+    const int64_t grid = std::min<int64_t>(R.count, resident);
+    if(grid <= 0) return cudaSuccess;
+    kern<<<static_cast<unsigned>(grid), kRowThreads + 32, smem, s>>>(b->p, R);
+    return cudaGetLastError();
+  }
+}
+
+// smallest staged width that holds the row (0: none)
+int row_k(int nx) {
+  for(int k : {2, 4})
+    if(nx <= 256 * k) return k;
+  return 0;
+}
+
+template <int LAT, int EQ, int ST>
+cudaError_t launch_rows(BoxState* b, bool odd, cudaStream_t s) {
+  using L = Lattice<LAT>;
+  using T = typename Store<ST>::T;
+  RowList R{};
+  int     nrows, nz;
+  if(odd) {
+    R.y0  = L::D > 1 ? 1 : 0;
+    nrows = L::D > 1 ? b->p.ny - 2 : b->p.ny;
+    R.z0  = L::D > 2 ? 1 : 0;
+    nz    = L::D > 2 ? b->p.nz - 2 : b->p.nz;
+  } else {
+    R.y0  = 0;
+    nrows = b->p.ny;
+    R.z0  = 0;
+    nz    = b->p.nz;
+  }
+  R.count    = (nrows > 0 && nz > 0) ? nrows * nz : 0;
+  R.nrows    = make_fastdiv(static_cast<uint32_t>(std::max(nrows, 1)));
+  R.err      = b->d_err;
+  R.limit_ns = b->wait_limit_ns;
+  R.starve   = b->wait_starve;
+  if(R.count == 0) return cudaSuccess;
+  const int k = row_k(b->p.nx);
+  if(k == 2) return odd ? launch_rows_one<LAT, EQ, ST, true, 2>(b, R, s) : launch_rows_one<LAT, EQ, ST, false, 2>(b, R, s);
+  if(k == 4) return odd ? launch_rows_one<LAT, EQ, ST, true, 4>(b, R, s) : launch_rows_one<LAT, EQ, ST, false, 4>(b, R, s);
+  return cudaErrorInvalidValue;
+}
+
+template <int LAT, class T>
+size_t rows_smem_for(int nx) {
+  const int k = row_k(nx);
+  if(k == 2) return row_smem<LAT, T, 2>();
+  if(k == 4) return row_smem<LAT, T, 4>();
+  return 0;
+}
+
+}  // namespace
+
+bool box_rows_supported(const BoxState* b) {
+  // every staged row starts on a 16-byte boundary (planes are padded to 128
+  // cells, so rows are aligned when nx * sizeof(storage) is), the halo keeps
+  // the odd step's loads 16-byte aligned too, and the stages fit shared memory
+  if(!b->d_err) return false;
+  if((static_cast<size_t>(b->p.nx) * b->elem) % 16 != 0) return false;
+  if((static_cast<size_t>(b->p.nalloc) * b->elem) % 16 != 0) return false;
+  size_t smem = 0;
+  const int nx = b->p.nx;
+  switch(b->desc.lattice) {
+    case LBM_D2Q9:
+      smem = b->elem == 8 ? rows_smem_for<LBM_D2Q9, double>(nx) : b->elem == 4 ? rows_smem_for<LBM_D2Q9, float>(nx) : rows_smem_for<LBM_D2Q9, uint16_t>(nx);
+      break;
+    case LBM_D3Q19:
+      smem = b->elem == 8 ? rows_smem_for<LBM_D3Q19, double>(nx) : b->elem == 4 ? rows_smem_for<LBM_D3Q19, float>(nx) : rows_smem_for<LBM_D3Q19, uint16_t>(nx);
+      break;
+    case LBM_D3Q7:
+      smem = b->elem == 8 ? rows_smem_for<LBM_D3Q7, double>(nx) : rows_smem_for<LBM_D3Q7, float>(nx);
+      break;
+    default: return false;
+  }
+  return smem > 0 && smem <= kRowSmemMax;
+}
+
+cudaError_t box_rows_bulk(BoxState* b, bool odd, cudaStream_t s) {
+  const int key = b->desc.lattice * 100 + b->desc.equation * 10 + b->desc.storage;
+  switch(key) {
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F64>(b, odd, s);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F32>(b, odd, s);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(b, odd, s);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(b, odd, s);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F64>(b, odd, s);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F32>(b, odd, s);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(b, odd, s);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(b, odd, s);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F64>(b, odd, s);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F32>(b, odd, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace lbm

@@ -21,14 +21,16 @@
 // The odd step covers the cells of the per-thread bulk kernel (interior fluid
 // cells with no solid neighbour, on rows 1..n-2); the boundary-list kernel of
 // box.cu handles the rest afterwards.  Every mbarrier wait is bounded: after
-// kWaitLimitNs the CTA records an error flag, waits (bounded again) for its
-// own copies still in flight and returns; the host reports the flag.
+// the wait limit (0.5 s unless a test lowers it) the CTA records an error
+// flag, waits (bounded again, kDrainLimitNs) for its own copies still in
+// flight and returns; the host reports the flag as LBM_ERR_TIMEOUT.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
 #include "box.h"
 #include "box_device.cuh"
+#include "bulk_copy.cuh"
 #include "lattice.cuh"
 #include "step_common.cuh"
 
@@ -36,75 +38,11 @@ namespace lbm {
 namespace {
 
 constexpr int      kSeg        = 256;          // cells per segment = threads per CTA
-constexpr uint64_t kWaitLimitNs = 500000000ull;  // 0.5 s per wait
 
 template <class T>
 constexpr int stages() {
   return sizeof(T) >= 8 ? 2 : 4;
 }
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// wait for phase `parity` of the barrier, giving up after kWaitLimitNs
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-  if(mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  while(!mbar_try_wait(bar, parity))
-    if(global_ns() - t0 > kWaitLimitNs) return false;
-  return true;
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src),
-               "r"(bytes), "r"(bar)
-               : "memory");
-}
-
-// n / d for n < 2^31 by multiply-high (Granlund-Montgomery, round-up
-// multiplier): d fixed per launch, m and l set on the host
-struct FastDiv {
-  uint32_t d, m;
-  int      l;
-};
-
-inline FastDiv make_fastdiv(uint32_t d) {
-  int l = 0;
-  while((uint64_t(1) << l) < d) ++l;
-  const uint64_t m = ((uint64_t(1) << 32) * ((uint64_t(1) << l) - d)) / d + 1;
-  return FastDiv{d, static_cast<uint32_t>(m), l};
-}
-
-__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) { return (__umulhi(n, f.m) + n) >> f.l; }
 
 struct SegList {
   FastDiv spr;      // segments per row, ceil(nx / kSeg)
@@ -112,6 +50,8 @@ struct SegList {
   int     y0, z0;   // first row: y in [y0, y0 + nrows), z from z0
   int     nseg;     // segments in the list
   int*    err;      // set to 1 when a wait times out
+  uint64_t limit_ns;  // limit of each pipeline wait
+  int     starve;   // test only: the producer never arms the CTA's first segment, so the waits on it run out
 };
 
 constexpr int kConsumers = kSeg / 32;  // consumer warps; warp 0 issues the copies
@@ -178,15 +118,15 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
   if(warp == 0) {
     // ---- producer ----
     if(lane == 0) {
+      int issued = 0;  // segments [0, issued) are armed (all but a starved one)
       for(int i = 0; i < nloc; ++i) {
         const int st = i % NST;
-        if(i >= NST && !mbar_wait_bounded(smem_u32(&empty[st]), static_cast<uint32_t>((i / NST - 1) & 1))) {
+        if(i >= NST && !mbar_wait_bounded(smem_u32(&empty[st]), static_cast<uint32_t>((i / NST - 1) & 1), W.limit_ns)) {
           atomicExch(W.err, 1);
-          // copies already issued may still land: wait for them (bounded)
-          for(int j = i - NST; j < i; ++j)
-            if(j >= 0) mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1));
           break;
         }
+        issued = i + 1;
+        if(W.starve && i == 0) continue;  // test only: nothing arms full[0], its waits run out
         int x0, y, z;
         coords(i, x0, y, z);
         const int      lo    = ODD ? max(x0 - HALO, 0) : x0;
@@ -204,6 +144,13 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
           bulk_g2s(smem_u32(dst0 + q * ROW), src, bytes, b);
         });
       }
+      // every copy this CTA issued has landed before its threads can all
+      // exit, also when consumer warps left early after a wait ran out (the
+      // last NST armed segments; earlier ones were consumed before their
+      // stage was re-armed).  Completed phases return at once.
+      for(int j = issued > NST ? issued - NST : 0; j < issued; ++j)
+        if(!(W.starve && j == 0))
+          mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1), kDrainLimitNs);
     }
     return;
   }
@@ -232,7 +179,8 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
     if(work) prefetch_moments<C, MOM, NV>(P, cell, prev);
 
     // the wait result is made warp-uniform so the warp leaves together
-    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1)));
+    const bool ok =
+        __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1), W.limit_ns));
     if(!ok) {
       if(lane == 0) atomicExch(W.err, 1);
       return;
@@ -329,7 +277,9 @@ cudaError_t launch_tma(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* 
   W.nseg  = (nrows > 0 && nz > 0) ? spr * nrows * nz : 0;
   W.spr   = make_fastdiv(static_cast<uint32_t>(spr));
   W.nrows = make_fastdiv(static_cast<uint32_t>(std::max(nrows, 1)));
-  W.err   = b->d_err;
+  W.err      = b->d_err;
+  W.limit_ns = b->wait_limit_ns;
+  W.starve   = b->wait_starve;
   *slots = static_cast<int64_t>(W.nseg) * kConsumers;
   if(W.nseg == 0) return cudaSuccess;
   if(odd) {

@@ -40,12 +40,19 @@ extern "C" int lbm_gpu_residual_noalloc(const double* vars, const double* varsol
   if(dev < 0 || dev >= MAX_DEVICES) return LBM_ERR_UNSUPPORTED;
   double* scratch = nullptr;
   {
-    // set-up, once per device, with that device current: the address of the
-    // array in this device's copy of the module.  In host code the name
-    // g_noalloc_partials is only a host-side stand-in, so kernels must be
-    // given this address instead.
+    // the address of the array in this device's copy of the module.  In host
+    // code the name g_noalloc_partials is only a host-side stand-in, so
+    // kernels must be given this address instead.  It is looked up on the
+    // first call on a device and again on every call whose stream is not
+    // being captured: a device reset (cudaDeviceReset, or another library
+    // resetting the primary context) loads the module again, possibly at
+    // another address.  A call during stream capture uses the address of the
+    // last call outside capture on that device.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if(cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) return LBM_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if(!g_partials_addr[dev]) {
+    if(!g_partials_addr[dev] || cap == cudaStreamCaptureStatusNone) {
+      if(cap != cudaStreamCaptureStatusNone) return LBM_ERR_INVALID;  // first call on this device inside a capture
       void*       addr = nullptr;
       cudaError_t e    = cudaGetSymbolAddress(&addr, g_noalloc_partials);
       if(e != cudaSuccess || !addr) return LBM_ERR_CUDA;

@@ -13,6 +13,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import os
+import sys
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -303,16 +304,16 @@ class BoxSolver:
                     break
         return done, res
 
-    KERNELS = {"thread": 0, "staged": 1, "paired": 2}
+    KERNELS = {"thread": 0, "staged": 1, "paired": 2, "rows": 3}
 
     def kernel(self, kind: Optional[str] = None) -> str:
-        """The bulk step kernel in use ("thread", "staged" or "paired", or
+        """The bulk step kernel in use ("thread", "staged", "paired" or "rows", or
         "even/odd" when the autotuner chose one per step parity); with `kind`,
         switch both parities to it first (all give bit-identical results)."""
         sel = C.c_int32()
         check(self._lib.lbm_gpu_box_select_kernel(self.ctx, -1 if kind is None else self.KERNELS[kind], C.byref(sel)), self.ctx,
               "select_kernel")
-        names = {0: "thread", 1: "staged", 2: "paired"}
+        names = {0: "thread", 1: "staged", 2: "paired", 3: "rows"}
         if sel.value >= 0:
             return names[sel.value]
         ev, od = C.c_int32(), C.c_int32()
@@ -494,7 +495,14 @@ class LBMSolver:
             s_sol += float(np.linalg.norm(s))
             s_sol2 += float(np.dot(s, s))
             max_err = max(max_err, delta)
-        l2 = (math.sqrt(s_err2) / math.sqrt(s_sol2)) / math.pow(n, 1.0 / grid.ndim)
+        # the reference takes these roots with gcem::sqrt, which returns 0 for
+        # an argument below machine epsilon (external/gcem_incl/sqrt.hpp); a
+        # converged case with sum |e|^2 < 2.2e-16 then reports L2 = 0, kept
+        # here so that the reported errors are the reference's
+        def root(x: float) -> float:
+            return 0.0 if abs(x) < sys.float_info.epsilon else math.sqrt(x)
+
+        l2 = (root(s_err2) / root(s_sol2)) / math.pow(n, 1.0 / grid.ndim)
         gre = s_err / s_sol
         bounds = {"errorMax": float(cfg.get("errorMax", 1.0)), "errorL2": float(cfg.get("errorL2", 1.0)),
                   "errorGRE": float(cfg.get("errorGRE", 1.0))}

@@ -17,10 +17,18 @@
 #      (which includes src/lbm/solver.cpp) against a serial MPI stub
 #      (oracle/mpi_stub/mpi.h), and link oracle/_ref/ref_harness.
 #
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+#        oracle/build_ref.sh --root     print the reference root it would use
+# The root is the argument, else $LBM_REFERENCE_ROOT, else the checkout this
+# recipe was written against (/root/reference).  Exit status 3: no reference
+# sources there (nothing is built).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+if [ "${1:-}" = "--root" ]; then
+  echo "${LBM_REFERENCE_ROOT:-/root/reference}"
+  exit 0
+fi
+REF="${1:-${LBM_REFERENCE_ROOT:-/root/reference}}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/lbm" ]; then
   echo "reference sources not found at $REF" >&2

@@ -24,7 +24,14 @@
 // then writes the reference's line.csv into the working directory
 // (src/postprocess/postprocessing.h:87-119): the golden file of the line probe.
 //
-// Usage: ref_harness <config.json> <nsteps> <outdir> [--time] [--vtp]
+// With --run it instead calls the solver's own run() (src/lbm/solver.cpp:175-214):
+// the reference's loop with its convergence check, extra step and analytic
+// comparison (compareToAnalyticalResult, :387-482), which print the residual
+// and the errors to cerr0, here at 17 significant digits; <nsteps> is ignored.
+// It then prints one JSON line to stdout: the steps run (m_timeStep after the
+// loop) and whether the solution diverged.
+//
+// Usage: ref_harness <config.json> <nsteps> <outdir> [--time] [--vtp] [--run]
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -66,7 +73,8 @@ std::string jnum(double x) {
 }
 
 template <LBMethodType LBTYPE, LBEquationType EQ>
-int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const std::string& out, bool timing, bool vtp) {
+int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const std::string& out, bool timing, bool vtp,
+            bool runloop) {
   using S                 = LBMSolver<Debug_Level::no_debug, LBTYPE, EQ>;
   constexpr GInt NDIM     = S::NDIM;
   constexpr GInt NDIST    = S::NDIST;
@@ -85,6 +93,14 @@ int runCase(int argc, char** argv, const std::string& cfg, long nsteps, const st
   S solver(0, 1);
   solver.init(argc, argv, cfg);
   solver.transferGrid(gridgen.grid());
+
+  if(runloop) {
+    cerr0.precision(17);
+    solver.run();
+    std::cout << "{\"steps\": " << solver.m_timeStep << ", \"diverged\": " << (solver.m_diverged ? "true" : "false") << "}"
+              << std::endl;
+    return 0;
+  }
 
   solver.loadConfiguration();
   solver.allocateMemory();
@@ -192,10 +208,11 @@ int main(int argc, char** argv) {
   const std::string cfg    = argv[1];
   const long        nsteps = std::stol(argv[2]);
   const std::string out    = argv[3];
-  bool              timing = false, vtp = false;
+  bool              timing = false, vtp = false, runloop = false;
   for(int a = 4; a < argc; ++a) {
-    timing = timing || std::string(argv[a]) == "--time";
-    vtp    = vtp || std::string(argv[a]) == "--vtp";
+    timing  = timing || std::string(argv[a]) == "--time";
+    vtp     = vtp || std::string(argv[a]) == "--vtp";
+    runloop = runloop || std::string(argv[a]) == "--run";
   }
 
   int provided = 0;
@@ -219,13 +236,13 @@ int main(int argc, char** argv) {
 
   int rc = 1;
   if(model == "D2Q9" && equation == "navierstokes") {
-    rc = runCase<LBMethodType::D2Q9, LBEquationType::Navier_Stokes>(hargc, hargv, cfg, nsteps, out, timing, vtp);
+    rc = runCase<LBMethodType::D2Q9, LBEquationType::Navier_Stokes>(hargc, hargv, cfg, nsteps, out, timing, vtp, runloop);
   } else if(model == "D2Q9" && equation == "poisson") {
-    rc = runCase<LBMethodType::D2Q9, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
+    rc = runCase<LBMethodType::D2Q9, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp, runloop);
   } else if(model == "D2Q5" && equation == "poisson") {
-    rc = runCase<LBMethodType::D2Q5, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
+    rc = runCase<LBMethodType::D2Q5, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp, runloop);
   } else if(model == "D1Q3" && equation == "poisson") {
-    rc = runCase<LBMethodType::D1Q3, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp);
+    rc = runCase<LBMethodType::D1Q3, LBEquationType::Poisson>(hargc, hargv, cfg, nsteps, out, timing, vtp, runloop);
   } else {
     std::cerr << "unsupported model/equation " << model << "/" << equation << std::endl;
   }

@@ -25,7 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
-REF = os.environ.get("LBM_REFERENCE_ROOT", "/root/reference")
+# the reference checkout, as the build recipe of the harness resolves it
+REF = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), "--root"], capture_output=True, text=True,
+                     check=True).stdout.strip()
 
 # (fixture name, config path, step counts)
 CASES = [
@@ -34,16 +36,16 @@ CASES = [
     ("couette_bnd_bbDirichlet", ("ref", "test/couette/couette_bnd_bbDirichlet.json"), [50]),
     ("couette_bnd_eq", ("ref", "test/couette/couette_bnd_eq.json"), [50]),
     ("couette_bnd_eq2", ("ref", "test/couette/couette_bnd_eq2.json"), [50]),
-    ("couette_bnd_NEEM", ("ref", "test/couette/couette_bnd_NEEM.json"), [50]),
+    ("couette_bnd_NEEM", ("ref", "test/couette/couette_bnd_NEEM.json"), [50, 1000]),
     ("couette_bnd_NEBB", ("ref", "test/couette/couette_bnd_NEBB.json"), [50]),
-    ("poiseuille", ("ref", "test/poiseuille/poiseuille.json"), [1, 50]),
+    ("poiseuille", ("ref", "test/poiseuille/poiseuille.json"), [1, 50, 1000]),
     ("poiseuille_bnd", ("ref", "test/poiseuille/poiseuille_bnd.json"), [50]),
     ("poiseuille_bnd_eq", ("ref", "test/poiseuille/poiseuille_bnd_eq.json"), [50]),
     ("poiseuille_bnd_NEEM", ("ref", "test/poiseuille/poiseuille_bnd_NEEM.json"), [50]),
     ("poiseuille_bnd_NEBB", ("ref", "test/poiseuille/poiseuille_bnd_NEBB.json"), [50]),
     ("poiseuille_bnd_pressure", ("ref", "test/poiseuille/poiseuille_bnd_pressure.json"), [50]),
     ("poiseuille_bnd_pressure_neem2", ("ref", "test/poiseuille/poiseuille_bnd_pressure_neem2.json"), [50]),
-    ("poisson1D_reaction", ("ref", "test/poisson/poisson1D_reaction.json"), [50]),
+    ("poisson1D_reaction", ("ref", "test/poisson/poisson1D_reaction.json"), [50, 1000]),
     ("poisson1d_dh_small", ("own", "poisson1d_dh_small.json"), [1, 100]),
     ("poisson2d_d2q5_small", ("own", "poisson2d_d2q5_small.json"), [1, 100]),
     ("poisson2d_d2q9_reaction_small", ("own", "poisson2d_d2q9_reaction_small.json"), [100]),
@@ -62,7 +64,7 @@ CASES = [
     # the reference's 2D flow around an obstacle (box minus a circle, pressure
     # inlet / outlet, bounce-back walls) at level 5 instead of 8
     ("sphere_ns_l5", ("ref", "test/sphere/sphere_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}),
-     [1, 60]),
+     [1, 60, 1000]),
 ]
 
 
@@ -258,6 +260,59 @@ def write_hilbert_kat():
     print(f"hilbert_kat.json: {len(kat)} known answers")
 
 
+# the reference's analytic test suite (test/run.sh: every LBM case whose config
+# carries analyticalSolution): the reference's own run() to convergence, its
+# step count and its analytic errors (compareToAnalyticalResult,
+# src/lbm/solver.cpp:387-482) at 17 digits -> tests/golden/analytic_suite.json,
+# with each case's config (the GPU test builds the grid from it natively)
+ANALYTIC_CASES = [(n, ("ref", f"test/couette/{n}.json")) for n in (
+    "couette", "couette_bnd", "couette_bnd_bbDirichlet", "couette_bnd_eq", "couette_bnd_eq2", "couette_bnd_NEEM", "couette_bnd_NEBB",
+    "couette_bnd_eq_aligned")] + [(n, ("ref", f"test/poiseuille/{n}.json")) for n in (
+    "poiseuille", "poiseuille_bnd", "poiseuille_bnd_eq", "poiseuille_bnd_NEBB", "poiseuille_bnd_NEEM", "poiseuille_bnd_pressure_neem2",
+    "poiseuille_bnd_pressure")] + [(n, ("ref", f"test/poisson/{n}.json")) for n in (
+    "poisson1D", "poisson1D_reaction", "poisson2D_helmholtz")]
+
+
+def run_analytic(name, src):
+    import re
+    import time
+    cfg = load_config(src)
+    with tempfile.TemporaryDirectory() as tmp:
+        local_cfg = os.path.join(tmp, "case.json")
+        with open(local_cfg, "w") as fh:
+            json.dump(cfg, fh)
+        out = os.path.join(tmp, "out")
+        os.makedirs(out)
+        t0 = time.time()
+        p = subprocess.run([HARNESS, local_cfg, "0", out, "--run"], cwd=tmp, check=True, capture_output=True, text=True)
+        wall = time.time() - t0
+    res = json.loads(p.stdout.strip().splitlines()[-1])
+
+    def grab(label):
+        m = re.findall(re.escape(label) + r"\s*([-+0-9.eEinfa]+)", p.stderr)
+        return float(m[-1]) if m else None
+
+    entry = {"config": cfg, "steps": res["steps"], "diverged": res["diverged"], "converged_to": grab("Reached convergence to:"),
+             "max": grab("max. Error:"), "l2": grab("avg. L2:"), "gre": grab("global relative error:")}
+    print(f"{name}: {entry['steps']} steps, max {entry['max']}, L2 {entry['l2']}, GRE {entry['gre']} ({wall:.1f} s)", flush=True)
+    return entry
+
+
+def write_analytic(wanted=()):
+    path = os.path.join(HERE, "analytic_suite.json")
+    suite = {}
+    if os.path.exists(path):
+        with open(path) as fh:
+            suite = json.load(fh)
+    for name, src in ANALYTIC_CASES:
+        if wanted and name not in wanted and "analytic" not in wanted:
+            continue
+        suite[name] = run_analytic(name, src)
+        with open(path, "w") as fh:
+            json.dump(suite, fh, indent=1, sort_keys=True)
+            fh.write("\n")
+
+
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
@@ -268,6 +323,8 @@ def main(argv):
         write_hilbert_kat()
     if not wanted or "lpt" in wanted:
         write_lpt()
+    if not wanted or "analytic" in wanted or wanted & {n for n, _ in ANALYTIC_CASES}:
+        write_analytic(wanted)
     for name, src, steps in CASES:
         if wanted and name not in wanted:
             continue

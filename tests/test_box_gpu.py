@@ -104,7 +104,7 @@ def test_box_fp64_matches_oracle(case, steps):
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
-@pytest.mark.parametrize("kernel", ["thread", "staged"])
+@pytest.mark.parametrize("kernel", ["thread", "staged", "rows"])
 def test_box_fp64_each_bulk_kernel_matches_oracle(case, kernel):
     g, o = make_pair(case)
     try:
@@ -120,7 +120,7 @@ def test_box_fp64_each_bulk_kernel_matches_oracle(case, kernel):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16dev", "bf16dev"])
-@pytest.mark.parametrize("other", ["staged", "paired"])
+@pytest.mark.parametrize("other", ["staged", "paired", "rows"])
 def test_bulk_kernels_agree_bitwise(case, storage, other):
     a, _ = make_pair(case, storage)
     b, _ = make_pair(case, storage)

@@ -92,17 +92,37 @@ def test_bad_tables_fail_loudly():
     assert ei.value.code == -3
 
 
-def test_reference_run_loop_converges_on_couette():
-    """The reference's own analytic test: Couette flow with a moving bounce-back
-    lid reaches its steady profile within the reference's bounds
-    (test/couette/couette.json: errorMax 4e-11, errorL2 7e-10)."""
+ANALYTIC_SUITE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "analytic_suite.json")
+
+
+def _analytic_cases():
+    with open(ANALYTIC_SUITE) as fh:
+        return json.load(fh)
+
+
+@pytest.mark.parametrize("name", sorted(_analytic_cases()))
+def test_reference_analytic_suite(name):
+    """The reference's own analytic test suite (test/run.sh: every case whose
+    config carries analyticalSolution): LBMSolver.run() on the GPU, on the grid
+    built natively from the case's JSON config, converges after exactly the
+    reference's number of steps, passes the reference's bounds
+    (compareToAnalyticalResult, src/lbm/solver.cpp:387-482), and reports the
+    reference's own max / L2 / GRE errors to 1e-10 relative (the values the
+    reference's run() printed, tests/golden/analytic_suite.json)."""
     from lbm_gb300.solver import LBMSolver
-    meta, solver, grid, out, consts, bnds, forcing = load_case("couette_1")
-    s = LBMSolver(solver, grid)
+
+    e = _analytic_cases()[name]
+    s = LBMSolver.from_config(e["config"])
     res = s.run()
-    assert res["converged"], res
+    assert res["converged"] and not res["diverged"], res
+    assert res["steps"] == e["steps"], (res["steps"], e["steps"])
     cmp = s.compare_to_analytical()
     assert cmp["passed"], cmp
+    for k in ("max", "l2", "gre"):
+        ref = e[k]
+        if ref is None:
+            continue
+        assert abs(cmp[k] - ref) <= 1e-10 * abs(ref), (k, cmp[k], ref)
 
 
 @pytest.mark.parametrize("name", ["cavity_small_100", "poisson2d_helmholtz_small_100"])

@@ -54,3 +54,27 @@ def test_noalloc_rejects_too_many_variables():
     res = torch.zeros(9, dtype=torch.float64, device="cuda")
     rc = lib.lbm_gpu_residual_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(a.data_ptr()), 16, 9, C.c_void_p(res.data_ptr()), None)
     assert rc == -1
+
+
+def test_noalloc_residual_full_scratch_three_calls():
+    """Enough cells that the first pass runs the full 304 blocks, with the
+    full 8 variables: every slot of the fixed scratch array is written.  The
+    calls alternate between that size and a smaller one (fewer blocks), each
+    on fresh data, so a partial left over from an earlier call would show."""
+    torch = pytest.importorskip("torch")
+    lib = load()
+    stream = torch.cuda.current_stream()
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    for n, scale in ((700_001, 1.0), (100_003, 3.0), (700_001, 0.25)):
+        nvar = 8
+        a = torch.randn((nvar, n), dtype=torch.float64, device="cuda", generator=gen) * scale
+        b = torch.randn((nvar, n), dtype=torch.float64, device="cuda", generator=gen)
+        res = torch.full((nvar,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        rc = lib.lbm_gpu_residual_noalloc(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), n, nvar,
+                                          C.c_void_p(res.data_ptr()), C.c_void_p(stream.cuda_stream))
+        assert rc == 0
+        torch.cuda.synchronize()
+        expect = (a - b).abs().sum(dim=1).cpu().numpy()
+        got = res.cpu().numpy()
+        assert np.allclose(got, expect, rtol=1e-12, atol=0), (n, got, expect)
