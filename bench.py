@@ -198,44 +198,67 @@ def run_variant(storage, case, warmup, steps, device):
     return s, tot, ker, n
 
 
-def cavities_run(args):
+def cavities_run(args, dist=None):
     """The batched cavities (2048 D2Q9 lid-driven cavities, sides 32-512,
     Re 10-1000, FP32): device-timed steps of the whole batch, then a bounded
-    run with the convergence check (residual 1e-8, every 100 steps)."""
-    from lbm_gb300 import cases
+    run with the convergence check (residual 1e-8, every 100 steps).  Under
+    torchrun every rank takes a contiguous share of the cavities balanced by
+    cells (lbm_gb300.shard) and steps it on its own GPU; the job time is the
+    slowest rank's and the per-cavity results are gathered on every rank."""
+    import torch
+
+    from lbm_gb300 import cases, shard
     from lbm_gb300.solver import BatchSolver
 
     c = cases.cavities()
-    b = BatchSolver(c["sides"], 1.0 / c["tau"], c["lid"], "f32")
-    b.initial_condition()
-    b.step(args.warmup)
-    tot, ker, n = b.profile_steps(args.steps)
-    cells = b.ncells
+    sides, omegas = c["sides"], 1.0 / c["tau"]
+    area_all = sides.astype(np.int64) ** 2
+    world = dist.get_world_size() if dist is not None and dist.is_initialized() else 1
+    info = {}
+
+    def solve(lo, hi):
+        b = BatchSolver(sides[lo:hi], omegas[lo:hi], c["lid"], "f32")
+        b.initial_condition()
+        b.step(args.warmup)
+        if dist is not None and dist.is_initialized():
+            dist.barrier()
+        tot, ker, n = b.profile_steps(args.steps)
+        info.update(tot=tot, ker=ker, n=n, cells=b.ncells, tuning=b.tuning())
+        t0 = time.perf_counter()
+        steps = b.run(args.cavity_steps, 100, 1e-8, raise_on_divergence=False)
+        info["wall"] = time.perf_counter() - t0
+        out = {"steps": steps, "status": b.status(), "residual": b.residuals().max(axis=1)}
+        b.close()
+        return out
+
+    res_all = shard.run_sharded(area_all, solve, dist)
+    t = torch.tensor([info["tot"], info["wall"], info["ker"] / max(info["n"], 1)], dtype=torch.float64,
+                     device="cuda" if world > 1 else "cpu")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    tot, wall, kernel_avg_ms = (float(v) for v in t.tolist())
+    cells = int(area_all.sum())
     hbm, peak_kind = peaks()
     bpc = 2 * 9 * 4 + 0  # no flag byte: the geometry follows from the side
-    kernel_avg_ms = ker / n
-    area = c["sides"].astype(np.int64) ** 2
-    before = np.zeros(len(area), dtype=np.int64) + args.warmup + args.steps
-    t0 = time.perf_counter()
-    steps = b.run(args.cavity_steps, 100, 1e-8, raise_on_divergence=False)
-    wall = time.perf_counter() - t0
-    status = b.status()
-    res = b.residuals().max(axis=1)
-    ok = np.isfinite(res) & (status != b.DIVERGED)
+    before = np.zeros(len(area_all), dtype=np.int64) + args.warmup + args.steps
+    status, res, steps = res_all["status"], res_all["residual"], res_all["steps"]
+    ok = np.isfinite(res) & (status != BatchSolver.DIVERGED)
     res_q = [float(x) for x in np.percentile(res[ok], [0, 50, 90, 100])] if ok.any() else None
-    updates = float(np.sum((steps - before) * area))
-    grid, tpb = b.tuning()
-    b.close()
+    updates = float(np.sum((steps - before) * area_all))
+    grid, tpb = info["tuning"]
     return {"metric": "MLUPS (2048 batched D2Q9 lid-driven cavities, FP32)", "value": cells * args.steps / (tot / 1e3) / 1e6,
-            "unit": "MLUPS", "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps, "dtype": "f32",
+            "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps,
+            "dtype": "f32", "scaling": "strong",
             "config": {"workload": "2048 D2Q9 lid-driven cavities, sides U{32..512}, Re logU[10,1000], lid 0.1, FP32",
-                       "cells": cells, "bytes_per_cell": bpc, "grid": grid, "threads_per_block": tpb},
-            "roofline": {"bound": "hbm", "achieved": bpc * cells / (kernel_avg_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": bpc * cells / (kernel_avg_ms / 1e3) / 1e9 / hbm, "peak_kind": peak_kind, "kernel": "k_batch",
+                       "cells": cells, "bytes_per_cell": bpc, "grid": grid, "threads_per_block": tpb,
+                       "parallelism": f"cavities sharded over {world} GPUs (contiguous shares balanced by cells)" if world > 1
+                       else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": bpc * cells / world / (kernel_avg_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": bpc * cells / world / (kernel_avg_ms / 1e3) / 1e9 / hbm, "peak_kind": peak_kind, "kernel": "k_batch",
                          "kernel_avg_ms": kernel_avg_ms},
             "run": {"max_steps": args.cavity_steps, "wall_s": wall, "mlups": updates / wall / 1e6,
-                    "converged": int(np.sum(status == b.CONVERGED)), "diverged": int(np.sum(status == b.DIVERGED)),
-                    "of": int(len(area)), "final_residual_min_median_p90_max": res_q}}
+                    "converged": int(np.sum(status == BatchSolver.CONVERGED)), "diverged": int(np.sum(status == BatchSolver.DIVERGED)),
+                    "of": int(len(area_all)), "final_residual_min_median_p90_max": res_q}}
 
 
 def poisson_run(args):
@@ -425,6 +448,18 @@ def main():
         return
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "cavities" and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        # independent cavities sharded over the ranks (no device collective)
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        line = cavities_run(args, dist)
+        if dist.get_rank() == 0:
+            print(json.dumps(line))
+        dist.destroy_process_group()
+        return
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,

@@ -31,8 +31,10 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <new>
+#include <system_error>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -69,6 +71,21 @@ int dir_sign(int dir) { return (dir & 1) ? 1 : -1; }
 // thread each.  Every slice writes only its own outputs, so the result does
 // not depend on the number of threads.
 // LBM_GRID_THREADS sets the number of slices (1-16) regardless of size.
+// Run the tasks on threads of their own.  If the process cannot start a
+// thread (std::system_error, e.g. at its thread limit), the tasks not yet
+// started run on the calling thread instead: every caller's result is the
+// same for any split, so no error crosses the C boundary.
+void run_tasks(std::vector<std::function<void()>>& tasks) {
+  std::vector<std::thread> pool;
+  size_t                   started = 0;
+  try {
+    for(; started < tasks.size(); ++started) pool.emplace_back(tasks[started]);
+  } catch(const std::system_error&) {
+  }
+  for(size_t t = started; t < tasks.size(); ++t) tasks[t]();
+  for(auto& th : pool) th.join();
+}
+
 template <class F>
 void parallel_for(int64_t n, F fn, int* parts_out = nullptr) {
   const int64_t min_per_thread = 1 << 16;
@@ -83,9 +100,9 @@ void parallel_for(int64_t n, F fn, int* parts_out = nullptr) {
     fn(int64_t(0), n, 0);
     return;
   }
-  std::vector<std::thread> pool;
-  for(int t = 0; t < parts; ++t) pool.emplace_back(fn, n * t / parts, n * (t + 1) / parts, t);
-  for(auto& th : pool) th.join();
+  std::vector<std::function<void()>> tasks;
+  for(int t = 0; t < parts; ++t) tasks.emplace_back([&fn, n, t, parts]() { fn(n * t / parts, n * (t + 1) / parts, t); });
+  run_tasks(tasks);
 }
 
 // Main neighbours (the adjacent positions that hold a cell) and the boundary
@@ -258,15 +275,15 @@ int lbm_grid_create(int32_t ndim, int32_t level, const lbm_geom_desc* objs, int3
       &parts);
   // pairwise merges of neighbouring slices until one is left
   for(int width = 1; width < parts; width *= 2) {
-    std::vector<std::thread> pool;
+    std::vector<std::function<void()>> merges;
     for(int a = 0; a + width < parts; a += 2 * width)
-      pool.emplace_back([&, a, width]() {
+      merges.emplace_back([&, a, width]() {
         std::vector<Kept> merged(part[a].size() + part[a + width].size());
         std::merge(part[a].begin(), part[a].end(), part[a + width].begin(), part[a + width].end(), merged.begin(), by_key);
         part[a].swap(merged);
         std::vector<Kept>().swap(part[a + width]);
       });
-    for(auto& th : pool) th.join();
+    run_tasks(merges);
   }
   std::vector<Kept>& kept = part[0];
   if(kept.empty() || kept.size() >= (size_t(1) << 31)) {

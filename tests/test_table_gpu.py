@@ -104,8 +104,9 @@ def _analytic_cases():
 def test_reference_analytic_suite(name):
     """The reference's own analytic test suite (test/run.sh: every case whose
     config carries analyticalSolution): LBMSolver.run() on the GPU, on the grid
-    built natively from the case's JSON config, converges after exactly the
-    reference's number of steps, passes the reference's bounds
+    built natively from the case's JSON config, stops after exactly the
+    reference's number of steps (at convergence, or at maxSteps where the
+    reference does not converge either), passes the reference's bounds
     (compareToAnalyticalResult, src/lbm/solver.cpp:387-482), and reports the
     reference's own max / L2 / GRE errors to 1e-10 relative (the values the
     reference's run() printed, tests/golden/analytic_suite.json)."""
@@ -114,7 +115,8 @@ def test_reference_analytic_suite(name):
     e = _analytic_cases()[name]
     s = LBMSolver.from_config(e["config"])
     res = s.run()
-    assert res["converged"] and not res["diverged"], res
+    # the reference either reached its convergence criterion or ran to maxSteps
+    assert res["converged"] == (e["converged_to"] is not None) and not res["diverged"], res
     assert res["steps"] == e["steps"], (res["steps"], e["steps"])
     cmp = s.compare_to_analytical()
     assert cmp["passed"], cmp
