@@ -411,6 +411,77 @@ def lpt_run(args):
                              "sample": "1,000 particles x 100 steps, scalar Python restatement"}}
 
 
+def profile_case(args):
+    """A small case of one workload for ncu: set-up and autotuning first, then
+    the measured launches inside the NVTX range "profile" (capture them with
+    ncu --nvtx --nvtx-include "profile/")."""
+    import torch
+
+    rng = torch.cuda.nvtx
+    if args.profile_case in B_PER_CELL:
+        from lbm_gb300.solver import BoxSolver
+
+        case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
+        s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
+                      inlet_velocity=case["inlet"])
+        s.initial_condition()
+        if args.kernel:
+            s.kernel(args.kernel)
+        s.step(4)
+        s.synchronize()
+        rng.range_push("profile")
+        s.step(4)
+        s.synchronize()
+        rng.range_pop()
+        return {"profile_case": args.profile_case, "threads_per_block": s.threads_per_block(), "kernel": s.kernel(),
+                "cells": int(np.prod(case["shape"]))}
+    if args.profile_case == "cavities":
+        from lbm_gb300 import cases
+        from lbm_gb300.solver import BatchSolver
+
+        c = cases.cavities()
+        sides, om = c["sides"][:256], 1.0 / c["tau"][:256]
+        b = BatchSolver(sides, om, c["lid"], "f32")
+        b.initial_condition()
+        b.step(4)
+        torch.cuda.synchronize()
+        rng.range_push("profile")
+        b.step(4)
+        torch.cuda.synchronize()
+        rng.range_pop()
+        return {"profile_case": "cavities", "domains": 256, "cells": b.ncells, "tuning": b.tuning()}
+    if args.profile_case == "poisson":
+        from lbm_gb300 import cases
+        from lbm_gb300.solver import BoxSolver
+
+        c = cases.pb_spheres(256, seed=7)
+        g = BoxSolver(c["lattice"], c["shape"], c["omega"], "f32", pb_nonlinear=True, **cases.box_kwargs(c))
+        g.initial_condition()
+        if args.kernel:
+            g.kernel(args.kernel)
+        g.step(4)
+        g.synchronize()
+        rng.range_push("profile")
+        g.step(4)
+        g.synchronize()
+        rng.range_pop()
+        return {"profile_case": "poisson", "cells": 256 ** 3, "kernel": g.kernel()}
+    # the U-Net: one training step (forward, loss, backward) on a batch of 8
+    from lbm_gb300.warmstart import UNet
+
+    net = UNet(8, 128, 512, seed=1)
+    r = np.random.default_rng(3)
+    net.set_batch((r.normal(size=(8, 128, 512, 32)) * 0.5).astype(np.float32), r.normal(size=(8, 128, 512, 3)).astype(np.float32),
+                  np.ones((8, 128, 512), dtype=bool))
+    net.loss_and_grad()
+    torch.cuda.synchronize()
+    rng.range_push("profile")
+    loss = net.loss_and_grad()
+    torch.cuda.synchronize()
+    rng.range_pop()
+    return {"profile_case": "unet", "batch": 8, "shape": [128, 512], "loss": loss}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -428,23 +499,16 @@ def main():
     ap.add_argument("--ws-per-batch", type=int, default=32, help="warm start: training channels per Reynolds number")
     ap.add_argument("--ws-lr", type=float, default=1e-3, help="warm start: peak learning rate")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
-    ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL),
-                    help="run 4 steps of a 256x128x128 version of the workload in this storage and exit (for ncu captures)")
+    ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL) + ["cavities", "poisson", "unet"],
+                    help="a small case for ncu captures, its measured launches inside the NVTX range 'profile': 4 steps of "
+                         "a 256x128x128 version of the sphere workload in this storage; or 4 steps of 256 of the cavities; "
+                         "or 4 steps of the D3Q7 Poisson-Boltzmann 256^3 case (FP32); or one training step of the U-Net "
+                         "(batch 8, 128x512)")
     ap.add_argument("--kernel", default=None, choices=["thread", "staged", "paired", "rows"],
                     help="--profile-case: force this bulk kernel")
     args = ap.parse_args()
     if args.profile_case:
-        from lbm_gb300.solver import BoxSolver
-
-        case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
-        s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
-                      inlet_velocity=case["inlet"])
-        s.initial_condition()
-        if args.kernel:
-            s.kernel(args.kernel)
-        s.step(4)
-        s.synchronize()
-        print(json.dumps({"profile_case": args.profile_case, "threads_per_block": s.threads_per_block(), "kernel": s.kernel()}))
+        print(json.dumps(profile_case(args)))
         return
     if args.warmup < 3:
         args.warmup = 3

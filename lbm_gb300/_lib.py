@@ -41,7 +41,7 @@ class BoxDesc(C.Structure):
                 ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("face", C.c_int32 * 6), ("omega", C.c_double),
                 ("wall_velocity", (C.c_double * 3) * 6), ("body_force", C.c_double * 3), ("inlet_density", C.c_double),
                 ("inlet_velocity", C.c_double * 3), ("init_density", C.c_double), ("init_velocity", C.c_double * 3),
-                ("kappa_sq", C.c_double), ("pb_nonlinear", C.c_int32), ("reserved", C.c_int32)]
+                ("kappa_sq", C.c_double), ("pb_nonlinear", C.c_int32), ("no_shift", C.c_int32)]
 
 
 class BatchDesc(C.Structure):

@@ -37,14 +37,15 @@
 // (XFACE) in line.  Results are bitwise those of the per-thread kernel: the
 // same loads, collision and stores per cell.
 //
-// Pipeline per CTA: warp 0 lane 0 keeps stages of row loads in flight (full
-// barriers); eight consumer warps step the row in shared memory, fence it for
-// the async proxy and meet at a named barrier; consumer thread 0 then issues
-// the row's bulk stores, and once the previous row's stores have read their
-// stage it releases that stage (empty barrier).  Every mbarrier wait is
-// bounded; a timed-out wait sets the error flag, the consumers agree on it at
-// the named barrier and leave together after thread 0's stores completed, and
-// the producer lets its own loads land before it leaves.
+// Pipeline per CTA, three roles: warp 0 lane 0 keeps stages of row loads in
+// flight (full barriers); eight warps step the row in shared memory, fence
+// their writes for the async proxy and mark the row done (done barriers, one
+// arrival per warp); warp 1 lane 0 issues the row's bulk stores and, once
+// they have read the stage, hands it back to the loads (empty barriers).  So
+// neither the cell warps nor the loads wait for a store.  Every mbarrier wait
+// is bounded; a wait that runs out sets the error flag, and every role then
+// leaves within its own bounded waits, the loads and stores it issued having
+// landed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,6 +61,14 @@ namespace {
 
 constexpr int kRowWarps   = 8;               // consumer warps per CTA
 constexpr int kRowThreads = 32 * kRowWarps;  // consumer threads
+constexpr int kRowBlock   = kRowThreads + 64;  // + the load warp and the store warp
+
+#ifndef LBM_ROWS_STAGES_16
+#define LBM_ROWS_STAGES_16 4
+#endif
+#ifndef LBM_ROWS_CTAS_16
+#define LBM_ROWS_CTAS_16 2
+#endif
 
 // halo elements on either side of a staged row: one 16-byte vector
 template <class T>
@@ -69,7 +78,7 @@ constexpr int row_halo() {
 // pipeline stages per CTA
 template <class T>
 constexpr int row_stages() {
-  return sizeof(T) <= 2 ? 3 : 2;
+  return sizeof(T) <= 2 ? LBM_ROWS_STAGES_16 : 2;
 }
 // staged row width (elements) for rows of up to 256*K cells
 template <class T, int K>
@@ -78,7 +87,7 @@ constexpr int row_width() {
 }
 template <int LAT, class T, int K>
 constexpr size_t row_smem() {
-  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 2 * row_stages<T>();
+  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 3 * row_stages<T>();
 }
 constexpr size_t kRowSmemMax = 200 * 1024;
 
@@ -120,8 +129,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
   if(!any_special) {
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
-      else f[q] = S::load(bx[q * WR]);
+      if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)], P.shift_f[q]);
+      else f[q] = S::load(bx[q * WR], P.shift_f[q]);
     });
     collide<LAT, EQ, C>(P, f, nullptr);
   } else {
@@ -131,8 +140,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
     } else {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
-        else f[q] = S::load(bx[q * WR]);
+        if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)], P.shift_f[q]);
+        else f[q] = S::load(bx[q * WR], P.shift_f[q]);
       });
       if(type == LBM_CELL_OUTLET) {
         // links from beyond +x: what the upstream cell received (ghost plane)
@@ -140,7 +149,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
         const int NA = static_cast<int>(P.nalloc);
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], P.shift_f[q]);
         });
       }
       collide<LAT, EQ, C>(P, f, nullptr);
@@ -148,8 +157,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
   }
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    if constexpr(ODD) bx[q * WR + L::c(q, 0)] = S::store(f[q]);
-    else bx[L::opp(q) * WR] = S::store(f[q]);
+    if constexpr(ODD) bx[q * WR + L::c(q, 0)] = S::store(f[q], P.shift_f[q]);
+    else bx[L::opp(q) * WR] = S::store(f[q], P.shift_f[q]);
   });
 }
 
@@ -157,11 +166,11 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
 // memory allow)
 template <int ST>
 constexpr int row_min_ctas() {
-  return ST == LBM_STORE_F64 ? 1 : (ST == LBM_STORE_F32 ? 2 : 3);
+  return ST == LBM_STORE_F64 ? 1 : (ST == LBM_STORE_F32 ? 2 : LBM_ROWS_CTAS_16);
 }
 
 template <int LAT, int EQ, int ST, bool ODD, int K>
-__global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_rows(BoxParams P, RowList R) {
+__global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxParams P, RowList R) {
   using L             = Lattice<LAT>;
   using S             = Store<ST>;
   using T             = typename S::T;
@@ -172,8 +181,9 @@ __global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_ro
   constexpr int STAGE = Q * WR;  // staged elements per row
   extern __shared__ __align__(128) unsigned char smem[];
   T*        buf   = reinterpret_cast<T*>(smem);
-  uint64_t* full  = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);
-  uint64_t* empty = full + NST;
+  uint64_t* full  = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);  // loads landed
+  uint64_t* done  = full + NST;                                                   // consumers wrote the row
+  uint64_t* empty = done + NST;                                                   // stores read the stage
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G    = static_cast<int>(gridDim.x);
@@ -185,6 +195,7 @@ __global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_ro
 #pragma unroll
     for(int s = 0; s < NST; ++s) {
       mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&done[s]), kRowWarps);
       mbar_init(smem_u32(&empty[s]), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -203,7 +214,7 @@ __global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_ro
   };
 
   if(warp == 0) {
-    // ---- producer ----
+    // ---- loads: warp 0, lane 0 ----
     if(lane == 0) {
       const uint32_t bytes  = static_cast<uint32_t>((ODD ? nx + 2 * H : nx) * sizeof(T));
       int            issued = 0;  // rows [0, issued) are armed (all but a starved one)
@@ -236,39 +247,54 @@ __global__ void __launch_bounds__(kRowThreads + 32, row_min_ctas<ST>()) k_box_ro
     return;
   }
 
-  // ---- consumers ----
-  const int tid = threadIdx.x - 32;
+  if(warp == 1) {
+    // ---- stores: warp 1, lane 0 ----
+    if(lane == 0) {
+      const uint32_t bytes = static_cast<uint32_t>(nx * sizeof(T));
+      for(int i = 0; i < nloc; ++i) {
+        const int st = i % NST;
+        if(!mbar_wait_bounded(smem_u32(&done[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns)) {
+          atomicExch(R.err, 1);
+          break;
+        }
+        int y, z;
+        coords(i, y, z);
+        const T* const stage = buf + st * STAGE + H;
+        static_for<Q>([&](auto qc) {
+          constexpr int p  = decltype(qc)::value;
+          const int     ys = ODD ? y + L::c(p, 1) : y;
+          const int     zs = ODD ? z + L::c(p, 2) : z;
+          bulk_s2g(A + p * NA + nx * (ys + ny * zs), smem_u32(stage + p * WR), bytes);
+        });
+        bulk_commit();
+        bulk_wait_read<0>();  // the stores have read the stage: hand it back to the loads
+        mbar_arrive(smem_u32(&empty[st]));
+      }
+      bulk_wait_all();  // every store this CTA issued has completed before it exits
+    }
+    return;
+  }
+
+  // ---- cells: warps 2 .. kRowWarps + 1 ----
+  const int tid = threadIdx.x - 64;
   for(int i = 0; i < nloc; ++i) {
     const int st = i % NST;
     int       y, z;
     coords(i, y, z);
-    const bool got = mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns);
-    if(!consumers_all(got, kRowThreads)) {  // every consumer leaves, or none
-      if(tid == 0) {
-        atomicExch(R.err, 1);
-        bulk_wait_all();  // the stores already issued complete before the CTA exits
-      }
+    // the wait result is made warp-uniform so the warp leaves together; a
+    // warp that leaves never marks its rows done, so the store warp's wait
+    // runs out too and nothing is stored from then on
+    if(!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns))) {
+      if(lane == 0) atomicExch(R.err, 1);
       return;
     }
     T* const stage = buf + st * STAGE + H;
 #pragma unroll 1
     for(int x = tid; x < nx; x += kRowThreads) row_cell<LAT, EQ, ST, ODD, WR>(P, stage + x, x, y, z);
     fence_async_smem();  // this thread's writes are visible to the bulk stores
-    consumers_sync(kRowThreads);
-    if(tid == 0) {
-      const uint32_t bytes = static_cast<uint32_t>(nx * sizeof(T));
-      static_for<Q>([&](auto qc) {
-        constexpr int p  = decltype(qc)::value;
-        const int     ys = ODD ? y + L::c(p, 1) : y;
-        const int     zs = ODD ? z + L::c(p, 2) : z;
-        bulk_s2g(A + p * NA + nx * (ys + ny * zs), smem_u32(stage + p * WR), bytes);
-      });
-      bulk_commit();
-      bulk_wait_read<1>();  // the previous row's stores have read their stage: release it
-      if(i > 0) mbar_arrive(smem_u32(&empty[(i - 1) % NST]));
-    }
+    __syncwarp();
+    if(lane == 0) mbar_arrive(smem_u32(&done[st]));
   }
-  if(tid == 0) bulk_wait_all();
 }
 
 template <int LAT, int EQ, int ST, bool ODD, int K>
@@ -285,7 +311,7 @@ cudaError_t launch_rows_one(BoxState* b, const RowList& R, cudaStream_t s) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
       if(e != cudaSuccess) return e;
       int per_sm = 0;
-      e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRowThreads + 32, smem);
+      e          = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRowBlock, smem);
       if(e != cudaSuccess) return e;
       int dev = 0, sms = 0;
       cudaGetDevice(&dev);
@@ -294,7 +320,7 @@ cudaError_t launch_rows_one(BoxState* b, const RowList& R, cudaStream_t s) {
     }
     const int64_t grid = std::min<int64_t>(R.count, resident);
     if(grid <= 0) return cudaSuccess;
-    kern<<<static_cast<unsigned>(grid), kRowThreads + 32, smem, s>>>(b->p, R);
+    kern<<<static_cast<unsigned>(grid), kRowBlock, smem, s>>>(b->p, R);
     return cudaGetLastError();
   }
 }

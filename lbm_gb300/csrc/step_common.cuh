@@ -21,12 +21,20 @@ constexpr double STATE_SCALE = 4096.0;
 // ---- storage conversions ---------------------------------------------------
 template <int ST>
 struct Store;
+// load(v) / store(v): the stored value is the state itself.  load(v, k) /
+// store(v, k) (the dense-box engine): the 16-bit storages hold the state
+// minus k, the state of a reference equilibrium for the population's
+// direction, so that a population near that equilibrium is stored as a
+// small number with FP16's / BF16's relative rounding; the 32- and 64-bit
+// storages ignore k.
 template <>
 struct Store<LBM_STORE_F64> {
   using T = double;
   using C = double;
   static __device__ __forceinline__ C load(T v) { return v; }
   static __device__ __forceinline__ T store(C v) { return v; }
+  static __device__ __forceinline__ C load(T v, float) { return v; }
+  static __device__ __forceinline__ T store(C v, float) { return v; }
 };
 template <>
 struct Store<LBM_STORE_F32> {
@@ -34,6 +42,8 @@ struct Store<LBM_STORE_F32> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return v; }
   static __device__ __forceinline__ T store(C v) { return v; }
+  static __device__ __forceinline__ C load(T v, float) { return v; }
+  static __device__ __forceinline__ T store(C v, float) { return v; }
 };
 template <>
 struct Store<LBM_STORE_F16_DEV> {
@@ -41,6 +51,8 @@ struct Store<LBM_STORE_F16_DEV> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return __half2float(v); }
   static __device__ __forceinline__ T store(C v) { return __float2half_rn(v); }
+  static __device__ __forceinline__ C load(T v, float k) { return __half2float(v) + k; }
+  static __device__ __forceinline__ T store(C v, float k) { return __float2half_rn(v - k); }
 };
 template <>
 struct Store<LBM_STORE_BF16_DEV> {
@@ -48,6 +60,8 @@ struct Store<LBM_STORE_BF16_DEV> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return __bfloat162float(v); }
   static __device__ __forceinline__ T store(C v) { return __float2bfloat16_rn(v); }
+  static __device__ __forceinline__ C load(T v, float k) { return __bfloat162float(v) + k; }
+  static __device__ __forceinline__ T store(C v, float k) { return __float2bfloat16_rn(v - k); }
 };
 
 // state value <-> population f of direction q

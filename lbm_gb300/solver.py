@@ -149,7 +149,9 @@ class BoxSolver:
     def __init__(self, lattice: int, shape, omega: float, storage: str = "f64", faces=("wall",) * 6, flags=None,
                  wall_velocity=None, body_force=(0, 0, 0), inlet_velocity=(0, 0, 0), inlet_density=1.0,
                  init_density=1.0, init_velocity=(0, 0, 0), equation: int = rc.EQ_NAVIER_STOKES, kappa_sq: float = 0.0,
-                 pb_nonlinear: bool = True, dirichlet=None, device: int = 0):
+                 pb_nonlinear: bool = True, dirichlet=None, device: int = 0, shift: bool = True):
+        """shift: the 16-bit storages hold each population's scaled deviation
+        minus that of the free-stream equilibrium (lbm_box_desc.no_shift)."""
         lib = load()
         self._lib = lib
         self.ctx = None
@@ -175,6 +177,7 @@ class BoxSolver:
         d.init_velocity[:] = [float(x) for x in init_velocity]
         d.kappa_sq = kappa_sq
         d.pb_nonlinear = int(pb_nonlinear)
+        d.no_shift = 0 if shift else 1
         self.storage = STORAGE[storage]
         fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
         di = None if dirichlet is None else np.ascontiguousarray(dirichlet, dtype=np.float64).reshape(-1)
