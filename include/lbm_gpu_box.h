@@ -33,13 +33,15 @@ extern "C" {
 /* population storage */
 typedef enum lbm_storage {
   /* Navier-Stokes populations are held as the scaled deviation
-   * v_i = (f_i - w_i) / w_i * 2^12 in every storage; Poisson populations as
-   * f_i.  The 16-bit storages hold v_i - k_i, k_i the scaled deviation of the
-   * equilibrium at rho = 1 and the free-stream velocity (the inlet velocity
-   * where the box has inlet cells, else the initial velocity; its x
-   * component, when it has no other): populations near the free stream are
-   * then stored as small numbers, with FP16's relative rounding.  See
-   * lbm_box_desc.no_shift. */
+   * v_i = (f_i - w_i) / w_i * 2^12 (FP64 storage) or as that deviation
+   * shifted to the free stream, s_i = v_i - k_i (FP32 / FP16 / BF16 storage),
+   * k_i the scaled deviation of the equilibrium at rho = 1 and the
+   * free-stream velocity U: the inlet velocity where the box has inlet
+   * cells, else the initial velocity, when it points along x (else U = 0).
+   * The single-precision collision works on s_i, so that near the free
+   * stream both the stored values and every intermediate are small numbers
+   * with FP16's / FP32's relative rounding.  Poisson populations are held as
+   * f_i.  See lbm_box_desc.no_shift. */
   LBM_STORE_F64     = 0, /* FP64 storage, FP64 arithmetic (the plain method) */
   LBM_STORE_F32     = 1, /* FP32 storage, FP32 arithmetic */
   LBM_STORE_F16_DEV = 2, /* FP16 storage, FP32 arithmetic */
@@ -79,7 +81,7 @@ typedef struct lbm_box_desc {
   double  init_velocity[3];
   double  kappa_sq;         /* Poisson-Boltzmann: nabla^2 phi = kappa^2 sinh(phi) (or kappa^2 phi) */
   int32_t pb_nonlinear;     /* 1: sinh, 0: linear Debye-Hueckel */
-  int32_t no_shift;         /* 1: the 16-bit storages hold v_i itself (k_i = 0); 0 (default): v_i - k_i */
+  int32_t no_shift;         /* 1: U = 0 (the single-precision storages hold v_i itself); 0 (default): the free stream */
 } lbm_box_desc;
 
 /* flags: ncells bytes (NULL = all fluid); dirichlet: ncells potentials of the

@@ -94,7 +94,7 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
         // the outlet: links from beyond +x, the ghost plane
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], P.shift_f[q]);
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
         });
       }
       if(sf) {
@@ -107,11 +107,11 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
           constexpr int q = decltype(qc)::value;
           if constexpr(L::D > 1 && L::c(q, 1) != 0) {
             if(L::c(q, 1) == py)
-              f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 1>(q)) * NA - (L::c(q, 0) + sz * L::c(q, 2))], P.shift_f[mirror_axis<LAT, 1>(q)]);
+              f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 1>(q)) * NA - (L::c(q, 0) + sz * L::c(q, 2))]);
           }
           if constexpr(L::D > 2 && L::c(q, 2) != 0) {
             if(L::c(q, 2) == pz)
-              f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 2>(q)) * NA - (L::c(q, 0) + sy * L::c(q, 1))], P.shift_f[mirror_axis<LAT, 2>(q)]);
+              f[q] = S::load(Ac[L::opp(mirror_axis<LAT, 2>(q)) * NA - (L::c(q, 0) + sy * L::c(q, 1))]);
           }
         });
       }
@@ -121,7 +121,7 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
         // links from beyond +x: what the upstream cell received (ghost plane)
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], P.shift_f[q]);
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
         });
       }
     }
@@ -131,7 +131,7 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
   if constexpr(!ODD) {
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      Ac[L::opp(q) * NA] = S::store(f[q], P.shift_f[q]);
+      Ac[L::opp(q) * NA] = S::store(f[q]);
     });
   } else {
     const int  sy = P.nx, sz = P.nx * P.ny;
@@ -149,17 +149,17 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
       }
       if constexpr(XFP && L::D > 1 && L::c(q, 1) != 0) {
         if(L::c(q, 1) == -py) {  // leaves through the free-slip face: lands mirrored on the face
-          Ac[mirror_axis<LAT, 1>(q) * NA + L::c(q, 0) + sz * L::c(q, 2)] = S::store(f[q], P.shift_f[mirror_axis<LAT, 1>(q)]);
+          Ac[mirror_axis<LAT, 1>(q) * NA + L::c(q, 0) + sz * L::c(q, 2)] = S::store(f[q]);
           return;
         }
       }
       if constexpr(XFP && L::D > 2 && L::c(q, 2) != 0) {
         if(L::c(q, 2) == -pz) {
-          Ac[mirror_axis<LAT, 2>(q) * NA + L::c(q, 0) + sy * L::c(q, 1)] = S::store(f[q], P.shift_f[mirror_axis<LAT, 2>(q)]);
+          Ac[mirror_axis<LAT, 2>(q) * NA + L::c(q, 0) + sy * L::c(q, 1)] = S::store(f[q]);
           return;
         }
       }
-      Ac[q * NA + off] = S::store(f[q], P.shift_f[q]);
+      Ac[q * NA + off] = S::store(f[q]);
     });
   }
 }
@@ -194,14 +194,14 @@ __device__ __forceinline__ void bulk_cell(const BoxParams& P, int x, int y, int 
   if constexpr(!ODD) {
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      f[q]            = S::load(Ac[q * NA], P.shift_f[q]);
+      f[q]            = S::load(Ac[q * NA]);
     });
   } else {
     const int sy = P.nx, sz = P.nx * P.ny;
     static_for<Q>([&](auto qc) {
       constexpr int q   = decltype(qc)::value;
       const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-      f[q]              = S::load(Ac[L::opp(q) * NA - off], P.shift_f[q]);  // warp-uniform offset from the cell's base
+      f[q]              = S::load(Ac[L::opp(q) * NA - off]);  // warp-uniform offset from the cell's base
     });
   }
   C prev[NV];
@@ -266,36 +266,33 @@ __global__ void __maxnreg__(40) k_box_bulk_lean(BoxParams P) {
 // Two populations of adjacent cells as one aligned load / store.
 template <int ST>
 struct Pair;
-// (k: the shift of the 16-bit storages, as Store<ST>::load / store)
 template <>
 struct Pair<LBM_STORE_F32> {
-  static __device__ __forceinline__ void load(const float* p, float& a, float& b, float) {
+  static __device__ __forceinline__ void load(const float* p, float& a, float& b) {
     const float2 v = *reinterpret_cast<const float2*>(p);
     a              = v.x;
     b              = v.y;
   }
-  static __device__ __forceinline__ void store(float* p, float a, float b, float) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+  static __device__ __forceinline__ void store(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 };
 template <>
 struct Pair<LBM_STORE_F16_DEV> {
-  static __device__ __forceinline__ void load(const __half* p, float& a, float& b, float k) {
+  static __device__ __forceinline__ void load(const __half* p, float& a, float& b) {
     const float2 v = __half22float2(*reinterpret_cast<const __half2*>(p));
-    a              = v.x + k;
-    b              = v.y + k;
+    a              = v.x;
+    b              = v.y;
   }
-  static __device__ __forceinline__ void store(__half* p, float a, float b, float k) {
-    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a - k, b - k);
-  }
+  static __device__ __forceinline__ void store(__half* p, float a, float b) { *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b); }
 };
 template <>
 struct Pair<LBM_STORE_BF16_DEV> {
-  static __device__ __forceinline__ void load(const __nv_bfloat16* p, float& a, float& b, float k) {
+  static __device__ __forceinline__ void load(const __nv_bfloat16* p, float& a, float& b) {
     const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
-    a              = v.x + k;
-    b              = v.y + k;
+    a              = v.x;
+    b              = v.y;
   }
-  static __device__ __forceinline__ void store(__nv_bfloat16* p, float a, float b, float k) {
-    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a - k, b - k);
+  static __device__ __forceinline__ void store(__nv_bfloat16* p, float a, float b) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
   }
 };
 
@@ -337,15 +334,15 @@ __global__ void __launch_bounds__(256) k_box_pair(BoxParams P) {
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     if constexpr(!ODD) {
-      PR::load(Ac + q * NA, f0[q], f1[q], P.shift_f[q]);
+      PR::load(Ac + q * NA, f0[q], f1[q]);
     } else {
       const int off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
       const T*  src = Ac + (L::opp(q) * NA - off);
       if constexpr(L::c(q, 0) == 0) {
-        PR::load(src, f0[q], f1[q], P.shift_f[q]);
+        PR::load(src, f0[q], f1[q]);
       } else {
-        f0[q] = S::load(src[0], P.shift_f[q]);
-        f1[q] = S::load(src[1], P.shift_f[q]);
+        f0[q] = S::load(src[0]);
+        f1[q] = S::load(src[1]);
       }
     }
   });
@@ -354,15 +351,15 @@ __global__ void __launch_bounds__(256) k_box_pair(BoxParams P) {
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     if constexpr(!ODD) {
-      PR::store(Ac + L::opp(q) * NA, f0[q], f1[q], P.shift_f[q]);
+      PR::store(Ac + L::opp(q) * NA, f0[q], f1[q]);
     } else {
       const int off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
       T*        dst = Ac + (q * NA + off);
       if constexpr(L::c(q, 0) == 0) {
-        PR::store(dst, f0[q], f1[q], P.shift_f[q]);
+        PR::store(dst, f0[q], f1[q]);
       } else {
-        dst[0] = S::store(f0[q], P.shift_f[q]);
-        dst[1] = S::store(f1[q], P.shift_f[q]);
+        dst[0] = S::store(f0[q]);
+        dst[1] = S::store(f1[q]);
       }
     }
   });
@@ -373,8 +370,9 @@ __global__ void __launch_bounds__(256) k_box_pair(BoxParams P) {
 // (a neighbour's slot, the cell's own slot for a bounce, or the outlet ghost)
 // and dst[q*n+i] the slot the post-collision f_q is pushed to (-1: it leaves
 // through an open face).  corr_* hold the moving-wall momentum in state units
-// and, for the 16-bit storages, the change of shift of a bounced population
-// (only allocated when a wall moves or the storage is shifted).
+// and, for a state shifted to a free stream (FP32 / FP16 / BF16 storage), the
+// change of shift of a bounced population (only allocated when a wall moves
+// or the state is shifted).
 template <int LAT>
 __global__ void k_box_build_links(BoxParams P, const int32_t* list, int n, int32_t* src, int32_t* dst, double* corr_src,
                                   double* corr_dst) {
@@ -399,10 +397,10 @@ __global__ void k_box_build_links(BoxParams P, const int32_t* list, int n, int32
     else if(lq.kind == LINK_BOUNCE) d = L::opp(q) * NA + cell;
     dst[q * n + i] = static_cast<int32_t>(d);
     if(corr_src) {
-      // a bounced population changes direction, and with it the shift of the
-      // 16-bit storages: the pulled slot holds f_opp(q), the pushed slot
+      // a bounced population changes direction, and with it the shift of a
+      // shifted state: the pulled slot holds f_opp(q), the pushed slot
       // receives f_opp(q)
-      const double dk = static_cast<double>(P.shift_f[L::opp(q)]) - static_cast<double>(P.shift_f[q]);
+      const double dk = bounce_shift<LAT>(P, q);
       corr_src[q * n + i] = lp.kind == LINK_BOUNCE ? lp.corr + dk : 0.0;
       corr_dst[q * n + i] = lq.kind == LINK_BOUNCE ? lq.corr - dk : 0.0;
     }
@@ -480,7 +478,7 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
     } else {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        f[q]            = S::load(A[src[q * n + i]], P.shift_f[q]);
+        f[q]            = S::load(A[src[q * n + i]]);
         if(corr_src) f[q] += static_cast<C>(corr_src[q * n + i]);
       });
       collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
@@ -490,7 +488,7 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
     moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      if(dsts[q] >= 0) A[dsts[q]] = S::store(f[q], P.shift_f[q]);
+      if(dsts[q] >= 0) A[dsts[q]] = S::store(f[q]);
     });
   }
   if constexpr(MOM == 2) warp_partials<NV>(diff, P.partials, P.partial_stride, slot0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
@@ -526,7 +524,8 @@ __global__ void k_box_outlet(BoxParams P) {
       } else {
         // bounce-back at the upstream cell (a wall or solid beside it)
         using C = typename S::C;
-        v = S::store(S::load(A[q * NA + u], P.shift_f[L::opp(q)]) + static_cast<C>(lk.corr), P.shift_f[q]);
+        // a bounced population changes direction, and with it the shift
+        v = S::store(S::load(A[q * NA + u]) + static_cast<C>(bounce_shift<LAT>(P, q) + lk.corr));
       }
     }
     A[Q * NA + ghost_index(P, q, y, z)] = v;
@@ -559,8 +558,8 @@ __device__ __forceinline__ void readout_cell(const BoxParams& P, bool odd, int x
 #pragma unroll
     for(int q = 0; q < Q; ++q) {
       if(!odd) {
-        f[q] = S::load(A[q * NA + cell], P.shift_f[q]);
-        if(type == LBM_CELL_OUTLET && L::c(q, 0) < 0) f[q] = S::load(A[q * NA + cell - 1], P.shift_f[q]);
+        f[q] = S::load(A[q * NA + cell]);
+        if(type == LBM_CELL_OUTLET && L::c(q, 0) < 0) f[q] = S::load(A[q * NA + cell - 1]);
       } else {
         int  xs = x;
         Link lk = resolve<LAT>(P, x, y, z, q, -1, q);
@@ -569,13 +568,14 @@ __device__ __forceinline__ void readout_cell(const BoxParams& P, bool odd, int x
           lk = resolve<LAT>(P, xs, y, z, q, -1, q);
         }
         const int64_t own = xs + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
-        if(lk.kind == LINK_CELL) f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell], P.shift_f[lk.q]);
-        else f[q] = S::load(A[q * NA + own], P.shift_f[L::opp(q)]) + static_cast<C>(lk.corr);  // bounced: f_opp(q) of the cell
+        if(lk.kind == LINK_CELL) f[q] = S::load(A[L::opp(lk.q) * NA + lk.cell]);
+        else  // bounced: f_opp(q) of the cell, with its change of shift
+          f[q] = S::load(A[q * NA + own]) + static_cast<C>(bounce_shift<LAT>(P, q) + lk.corr);
       }
     }
   }
 #pragma unroll
-  for(int q = 0; q < Q; ++q) out[q * stride] = state_to_f<LAT, EQ>(static_cast<double>(f[q]), q);
+  for(int q = 0; q < Q; ++q) out[q * stride] = box_state_to_f<LAT, EQ, ST>(P, static_cast<double>(f[q]), q);
 }
 
 template <int LAT, int EQ, int ST>
@@ -604,7 +604,7 @@ __global__ void k_box_load(BoxParams P, const double* in) {
 #pragma unroll
   for(int q = 0; q < Q; ++q) v[q] = in[q * P.ncells + cell];
 #pragma unroll
-  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(v[q], q)), P.shift_f[q]);
+  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(box_f_to_state<LAT, EQ, ST>(P, v[q], q)));
 }
 
 // uniform initial state: the same FP64 population vector in every cell
@@ -622,7 +622,7 @@ __global__ void k_box_init(BoxParams P, InitVec v) {
   if(cell >= P.ncells) return;
   T* A = static_cast<T*>(P.pop);
 #pragma unroll
-  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(f_to_state<LAT, EQ>(v.f[q], q)), P.shift_f[q]);
+  for(int q = 0; q < Q; ++q) A[q * P.nalloc + cell] = S::store(static_cast<C>(box_f_to_state<LAT, EQ, ST>(P, v.f[q], q)));
 }
 
 // moments (rho or phi, u) of FP64 populations
@@ -1284,21 +1284,20 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
     p.force_f[d]   = static_cast<float>(p.force[d]);
     p.inlet_u_f[d] = static_cast<float>(p.inlet_u[d]);
   }
-  // the 16-bit storages hold each population's scaled deviation minus that of
-  // the equilibrium at rho = 1 and the free-stream velocity: the inlet
-  // velocity where the box has inlet cells, else the initial velocity.  Only
-  // a velocity along x is used (0 otherwise): every direction then has the
-  // same shift as its reflection in a y or z face, so free-slip reflections
-  // keep the stored value, and only bounce-back changes it.
-  for(int q = 0; q < 19; ++q) p.shift_f[q] = 0.0f;
-  if(eq == LBM_NAVIER_STOKES && (st == LBM_STORE_F16_DEV || st == LBM_STORE_BF16_DEV) && !desc->no_shift) {
+  // the FP32 / FP16 / BF16 Navier-Stokes state is shifted to the free
+  // stream: each population's scaled deviation minus that of the equilibrium
+  // at rho = 1 and the free-stream velocity U (the inlet velocity where the
+  // box has inlet cells, else the initial velocity), and the single-precision
+  // collision works on that state (collide_ns_shifted).  Only a velocity along
+  // x is used (U = 0 otherwise): every direction then has the same shift as
+  // its reflection in a y or z face, so free-slip reflections keep the state,
+  // and only bounce-back changes it (bounce_shift).
+  p.shift_u   = 0.0f;
+  p.shift_u_d = 0.0;
+  if(eq == LBM_NAVIER_STOKES && st != LBM_STORE_F64 && !desc->no_shift) {
     const double* uref = has_inlet ? desc->inlet_velocity : desc->init_velocity;
-    const double  u    = (uref[1] == 0.0 && uref[2] == 0.0) ? uref[0] : 0.0;
-    for(int q = 0; q < b->Q; ++q) {
-      const int    cx = lat == LBM_D2Q9 ? Lattice<LBM_D2Q9>::c(q, 0) : Lattice<LBM_D3Q19>::c(q, 0);
-      const double cu = cx * u;
-      p.shift_f[q]    = static_cast<float>(STATE_SCALE * (3.0 * cu + 4.5 * cu * cu - 1.5 * u * u));
-    }
+    p.shift_u          = (uref[1] == 0.0 && uref[2] == 0.0) ? static_cast<float>(uref[0]) : 0.0f;
+    p.shift_u_d        = p.shift_u;  // the arithmetic's U, exactly
   }
 
   // one guard plane in front: the odd step issues its pull loads before it
@@ -1394,8 +1393,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   for(int i = 0; i < 6; ++i)
     for(int d = 0; d < 3; ++d)
       if(desc->wall_velocity[i][d] != 0.0 && desc->face[i] == LBM_FACE_WALL) moving = true;
-  for(int q = 0; q < b->Q; ++q)
-    if(p.shift_f[q] != 0.0f) moving = true;  // shifted storage: bounced populations change shift
+  if(p.shift_u != 0.0f) moving = true;  // shifted state: bounced populations change shift
   if(e == cudaSuccess && b->n_bnd > 0) {
     const size_t nl = static_cast<size_t>(b->n_bnd) * b->Q;
     e = cudaMalloc(&b->link_src, sizeof(int32_t) * nl);

@@ -37,11 +37,13 @@ struct BoxParams {
   // pipe is narrow: converting a double parameter per cell is measurable)
   float   omega_f, force_f[3], inlet_rho_f, inlet_u_f[3], pb_src_f;
   int     has_outlet;
-  // 16-bit storages: the stored value of a population of direction q is its
-  // scaled deviation minus shift_f[q], the scaled deviation of the
-  // equilibrium at rho = 1 and the reference velocity (0 for the other
-  // storages and for Poisson)
-  float   shift_f[19];
+  // FP32 / FP16 / BF16 storage of Navier-Stokes populations: the state is
+  // the scaled deviation shifted to the free stream U = (shift_u, 0, 0),
+  // s_q = v_q - S P_q(U), S P_q(U) the scaled deviation of the equilibrium at
+  // rho = 1 and u = U (0 for FP64 storage, for Poisson and without a free
+  // stream); shift_u_d: the same U in double precision
+  float   shift_u;
+  double  shift_u_d;
   const uint8_t* flags;     // ncells
   const double*  dirichlet; // ncells Poisson Dirichlet values or nullptr
   void*   pop;              // Q planes of nalloc values of the storage type

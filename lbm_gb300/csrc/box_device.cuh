@@ -110,6 +110,31 @@ __device__ __forceinline__ Link resolve(const BoxParams& P, int x, int y, int z,
   return Link{LINK_CELL, cell, mask ? mirror<LAT>(q, mask) : q, 0.0};
 }
 
+// The shift of the FP32 / FP16 / BF16 Navier-Stokes state (s_q = v_q -
+// S P_q(U), box.h), FP64: the shift of direction q, and K_opp(q) - K_q, the
+// change of shift of a population bounced from direction q into opp(q).
+template <int LAT>
+__device__ __forceinline__ double state_shift(const BoxParams& P, int q) {
+  const double U = P.shift_u_d, cu = Lattice<LAT>::c(q, 0) * U;
+  return STATE_SCALE * (3.0 * cu + 4.5 * cu * cu - 1.5 * U * U);
+}
+template <int LAT>
+__device__ __forceinline__ double bounce_shift(const BoxParams& P, int q) {
+  return -6.0 * STATE_SCALE * Lattice<LAT>::c(q, 0) * P.shift_u_d;
+}
+// state of a box <-> population f (FP64), with the shift
+template <int LAT, int EQ, int ST>
+__device__ __forceinline__ double box_state_to_f(const BoxParams& P, double s, int q) {
+  if constexpr(EQ == LBM_NAVIER_STOKES && ST != LBM_STORE_F64) s += state_shift<LAT>(P, q);
+  return state_to_f<LAT, EQ>(s, q);
+}
+template <int LAT, int EQ, int ST>
+__device__ __forceinline__ double box_f_to_state(const BoxParams& P, double f, int q) {
+  double s = f_to_state<LAT, EQ>(f, q);
+  if constexpr(EQ == LBM_NAVIER_STOKES && ST != LBM_STORE_F64) s -= state_shift<LAT>(P, q);
+  return s;
+}
+
 template <int LAT>
 __device__ __forceinline__ int64_t offset(const BoxParams& P, int q) {
   using L = Lattice<LAT>;
@@ -130,6 +155,9 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
   return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
 }
 
+// The collision of one cell.  FP64 arithmetic (FP64 storage) works on the
+// scaled deviation v; FP32 arithmetic (the other storages) on the state
+// shifted to the free stream (collide_ns_shifted, U = P.shift_u).
 template <int LAT, int EQ, class C>
 __device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
   if constexpr(EQ == LBM_NAVIER_STOKES) {
@@ -137,8 +165,13 @@ __device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
     F[0] = prm<C>(P.force[0], P.force_f[0]);
     F[1] = prm<C>(P.force[1], P.force_f[1]);
     F[2] = prm<C>(P.force[2], P.force_f[2]);
-    if(P.has_force) collide_ns<LAT, C, true>(prm<C>(P.omega, P.omega_f), true, F, v, mom_out);
-    else collide_ns<LAT, C, false>(prm<C>(P.omega, P.omega_f), false, F, v, mom_out);
+    if constexpr(sizeof(C) == 4) {
+      if(P.has_force) collide_ns_shifted<LAT, true>(P.omega_f, true, F, P.shift_u, v, mom_out);
+      else collide_ns_shifted<LAT, false>(P.omega_f, false, F, P.shift_u, v, mom_out);
+    } else {
+      if(P.has_force) collide_ns<LAT, C, true>(prm<C>(P.omega, P.omega_f), true, F, v, mom_out);
+      else collide_ns<LAT, C, false>(prm<C>(P.omega, P.omega_f), false, F, v, mom_out);
+    }
   } else {
     collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
                             mom_out);
@@ -150,7 +183,10 @@ template <int LAT, int EQ, class C>
 __device__ __forceinline__ void emit_equilibrium(const BoxParams& P, C* v, int64_t cell) {
   using L         = Lattice<LAT>;
   constexpr int Q = L::Q, D = L::D;
-  if constexpr(EQ == LBM_NAVIER_STOKES) {
+  if constexpr(EQ == LBM_NAVIER_STOKES && sizeof(C) == 4) {
+    const float ui[3] = {P.inlet_u_f[0], P.inlet_u_f[1], P.inlet_u_f[2]};
+    equilibrium_shifted<LAT>(P.inlet_rho_f, ui, P.shift_u, v);
+  } else if constexpr(EQ == LBM_NAVIER_STOKES) {
     const C rho = prm<C>(P.inlet_rho, P.inlet_rho_f);
     C       ui[3];
     static_for<D>([&](auto dc) { ui[decltype(dc)::value] = prm<C>(P.inlet_u[decltype(dc)::value], P.inlet_u_f[decltype(dc)::value]); });

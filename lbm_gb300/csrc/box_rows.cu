@@ -37,15 +37,14 @@
 // (XFACE) in line.  Results are bitwise those of the per-thread kernel: the
 // same loads, collision and stores per cell.
 //
-// Pipeline per CTA, three roles: warp 0 lane 0 keeps stages of row loads in
-// flight (full barriers); eight warps step the row in shared memory, fence
-// their writes for the async proxy and mark the row done (done barriers, one
-// arrival per warp); warp 1 lane 0 issues the row's bulk stores and, once
-// they have read the stage, hands it back to the loads (empty barriers).  So
-// neither the cell warps nor the loads wait for a store.  Every mbarrier wait
-// is bounded; a wait that runs out sets the error flag, and every role then
-// leaves within its own bounded waits, the loads and stores it issued having
-// landed.
+// Pipeline per CTA: warp 0 lane 0 issues every copy.  It keeps NST rows of
+// loads in flight (full barriers); eight cell warps step a loaded row in
+// shared memory, fence their writes for the async proxy and mark it done
+// (done barriers, one arrival per warp); the copy thread then issues the
+// row's bulk stores and, once they have read the stage, loads the next row
+// into it.  The cell warps never wait for a store.  Every mbarrier wait is
+// bounded; a wait that runs out sets the error flag, and every role then
+// leaves within its own bounded waits, the copies it issued having landed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -61,13 +60,13 @@ namespace {
 
 constexpr int kRowWarps   = 8;               // consumer warps per CTA
 constexpr int kRowThreads = 32 * kRowWarps;  // consumer threads
-constexpr int kRowBlock   = kRowThreads + 64;  // + the load warp and the store warp
+constexpr int kRowBlock   = kRowThreads + 32;  // + the copy warp
 
 #ifndef LBM_ROWS_STAGES_16
-#define LBM_ROWS_STAGES_16 4
+#define LBM_ROWS_STAGES_16 3
 #endif
 #ifndef LBM_ROWS_CTAS_16
-#define LBM_ROWS_CTAS_16 2
+#define LBM_ROWS_CTAS_16 3
 #endif
 
 // halo elements on either side of a staged row: one 16-byte vector
@@ -87,7 +86,7 @@ constexpr int row_width() {
 }
 template <int LAT, class T, int K>
 constexpr size_t row_smem() {
-  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 3 * row_stages<T>();
+  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 2 * row_stages<T>();
 }
 constexpr size_t kRowSmemMax = 200 * 1024;
 
@@ -129,8 +128,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
   if(!any_special) {
     static_for<Q>([&](auto qc) {
       constexpr int q = decltype(qc)::value;
-      if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)], P.shift_f[q]);
-      else f[q] = S::load(bx[q * WR], P.shift_f[q]);
+      if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
+      else f[q] = S::load(bx[q * WR]);
     });
     collide<LAT, EQ, C>(P, f, nullptr);
   } else {
@@ -140,8 +139,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
     } else {
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)], P.shift_f[q]);
-        else f[q] = S::load(bx[q * WR], P.shift_f[q]);
+        if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
+        else f[q] = S::load(bx[q * WR]);
       });
       if(type == LBM_CELL_OUTLET) {
         // links from beyond +x: what the upstream cell received (ghost plane)
@@ -149,7 +148,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
         const int NA = static_cast<int>(P.nalloc);
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], P.shift_f[q]);
+          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
         });
       }
       collide<LAT, EQ, C>(P, f, nullptr);
@@ -157,8 +156,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
   }
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
-    if constexpr(ODD) bx[q * WR + L::c(q, 0)] = S::store(f[q], P.shift_f[q]);
-    else bx[L::opp(q) * WR] = S::store(f[q], P.shift_f[q]);
+    if constexpr(ODD) bx[q * WR + L::c(q, 0)] = S::store(f[q]);
+    else bx[L::opp(q) * WR] = S::store(f[q]);
   });
 }
 
@@ -180,10 +179,9 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
   constexpr int WR    = row_width<T, K>();
   constexpr int STAGE = Q * WR;  // staged elements per row
   extern __shared__ __align__(128) unsigned char smem[];
-  T*        buf   = reinterpret_cast<T*>(smem);
-  uint64_t* full  = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);  // loads landed
-  uint64_t* done  = full + NST;                                                   // consumers wrote the row
-  uint64_t* empty = done + NST;                                                   // stores read the stage
+  T*        buf  = reinterpret_cast<T*>(smem);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);  // the row's loads landed
+  uint64_t* done = full + NST;                                                   // the cell warps wrote the row
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G    = static_cast<int>(gridDim.x);
@@ -196,7 +194,6 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
     for(int s = 0; s < NST; ++s) {
       mbar_init(smem_u32(&full[s]), 1);
       mbar_init(smem_u32(&done[s]), kRowWarps);
-      mbar_init(smem_u32(&empty[s]), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -214,43 +211,29 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
   };
 
   if(warp == 0) {
-    // ---- loads: warp 0, lane 0 ----
+    // ---- copies: warp 0, lane 0 issues every load and every store ----
     if(lane == 0) {
-      const uint32_t bytes  = static_cast<uint32_t>((ODD ? nx + 2 * H : nx) * sizeof(T));
-      int            issued = 0;  // rows [0, issued) are armed (all but a starved one)
-      for(int i = 0; i < nloc; ++i) {
+      const uint32_t lbytes = static_cast<uint32_t>((ODD ? nx + 2 * H : nx) * sizeof(T));
+      const uint32_t sbytes = static_cast<uint32_t>(nx * sizeof(T));
+      auto           load   = [&](int i) {
         const int st = i % NST;
-        if(i >= NST && !mbar_wait_bounded(smem_u32(&empty[st]), static_cast<uint32_t>((i / NST - 1) & 1), R.limit_ns)) {
-          atomicExch(R.err, 1);
-          break;
-        }
-        issued = i + 1;
-        if(R.starve && i == 0) continue;  // test only: nothing arms full[0], its waits run out
-        int y, z;
+        int       y, z;
         coords(i, y, z);
         const uint32_t b = smem_u32(&full[st]);
-        mbar_expect_tx(b, bytes * Q);
+        mbar_expect_tx(b, lbytes * Q);
         T* const dst0 = buf + st * STAGE + (ODD ? 0 : H);
         static_for<Q>([&](auto qc) {
           constexpr int p  = decltype(qc)::value;
           const int     ys = ODD ? y + L::c(p, 1) : y;
           const int     zs = ODD ? z + L::c(p, 2) : z;
           const T*      src = A + p * NA + nx * (ys + ny * zs) - (ODD ? H : 0);
-          bulk_g2s(smem_u32(dst0 + p * WR), src, bytes, b);
+          bulk_g2s(smem_u32(dst0 + p * WR), src, lbytes, b);
         });
-      }
-      // every load this CTA issued has landed before its threads can all exit
-      for(int j = issued > NST ? issued - NST : 0; j < issued; ++j)
-        if(!(R.starve && j == 0))
-          mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1), kDrainLimitNs);
-    }
-    return;
-  }
-
-  if(warp == 1) {
-    // ---- stores: warp 1, lane 0 ----
-    if(lane == 0) {
-      const uint32_t bytes = static_cast<uint32_t>(nx * sizeof(T));
+      };
+      // rows [0, issued) are armed (all but a starved one)
+      int issued = 0;
+      for(; issued < nloc && issued < NST; ++issued)
+        if(!(R.starve && issued == 0)) load(issued);  // test only: nothing arms full[0], its waits run out
       for(int i = 0; i < nloc; ++i) {
         const int st = i % NST;
         if(!mbar_wait_bounded(smem_u32(&done[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns)) {
@@ -264,26 +247,33 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
           constexpr int p  = decltype(qc)::value;
           const int     ys = ODD ? y + L::c(p, 1) : y;
           const int     zs = ODD ? z + L::c(p, 2) : z;
-          bulk_s2g(A + p * NA + nx * (ys + ny * zs), smem_u32(stage + p * WR), bytes);
+          bulk_s2g(A + p * NA + nx * (ys + ny * zs), smem_u32(stage + p * WR), sbytes);
         });
         bulk_commit();
-        bulk_wait_read<0>();  // the stores have read the stage: hand it back to the loads
-        mbar_arrive(smem_u32(&empty[st]));
+        // the stage is free once its stores have read it; the cell warps are
+        // meanwhile on the rows already loaded
+        bulk_wait_read<0>();
+        if(issued < nloc) load(issued++);
       }
-      bulk_wait_all();  // every store this CTA issued has completed before it exits
+      bulk_wait_all();  // every store issued has completed
+      // and every load issued has landed before the CTA can exit (rows the
+      // cell warps did not take after a wait ran out)
+      for(int j = issued > NST ? issued - NST : 0; j < issued; ++j)
+        if(!(R.starve && j == 0))
+          mbar_wait_bounded(smem_u32(&full[j % NST]), static_cast<uint32_t>((j / NST) & 1), kDrainLimitNs);
     }
     return;
   }
 
-  // ---- cells: warps 2 .. kRowWarps + 1 ----
-  const int tid = threadIdx.x - 64;
+  // ---- cells: warps 1 .. kRowWarps ----
+  const int tid = threadIdx.x - 32;
   for(int i = 0; i < nloc; ++i) {
     const int st = i % NST;
     int       y, z;
     coords(i, y, z);
     // the wait result is made warp-uniform so the warp leaves together; a
-    // warp that leaves never marks its rows done, so the store warp's wait
-    // runs out too and nothing is stored from then on
+    // warp that leaves never marks its rows done, so the copy thread's wait
+    // runs out too and nothing more is loaded or stored
     if(!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[st]), static_cast<uint32_t>((i / NST) & 1), R.limit_ns))) {
       if(lane == 0) atomicExch(R.err, 1);
       return;

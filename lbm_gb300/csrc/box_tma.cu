@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
     if(work && !emit)
       static_for<Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        f[q]            = S::load(row[q * ROW - (ODD ? L::c(q, 0) : 0)], P.shift_f[q]);
+        f[q]            = S::load(row[q * ROW - (ODD ? L::c(q, 0) : 0)]);
       });
     __syncwarp();
     if(lane == 0) mbar_arrive(smem_u32(&empty[st]));  // this warp is done with the stage
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
           if(type == LBM_CELL_OUTLET) {
             static_for<Q>([&](auto qc) {
               constexpr int q = decltype(qc)::value;
-              if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))], P.shift_f[q]);
+              if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
             });
           }
         }
@@ -213,14 +213,14 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
       if constexpr(!ODD) {
         static_for<Q>([&](auto qc) {
           constexpr int q = decltype(qc)::value;
-          A[L::opp(q) * NA + cell] = S::store(f[q], P.shift_f[q]);
+          A[L::opp(q) * NA + cell] = S::store(f[q]);
         });
       } else {
         const int sy = nx, sz = nx * ny;
         static_for<Q>([&](auto qc) {
           constexpr int q   = decltype(qc)::value;
           const int     off = L::c(q, 0) + sy * L::c(q, 1) + sz * L::c(q, 2);
-          A[q * NA + cell + off] = S::store(f[q], P.shift_f[q]);
+          A[q * NA + cell + off] = S::store(f[q]);
         });
       }
     }

@@ -21,20 +21,12 @@ constexpr double STATE_SCALE = 4096.0;
 // ---- storage conversions ---------------------------------------------------
 template <int ST>
 struct Store;
-// load(v) / store(v): the stored value is the state itself.  load(v, k) /
-// store(v, k) (the dense-box engine): the 16-bit storages hold the state
-// minus k, the state of a reference equilibrium for the population's
-// direction, so that a population near that equilibrium is stored as a
-// small number with FP16's / BF16's relative rounding; the 32- and 64-bit
-// storages ignore k.
 template <>
 struct Store<LBM_STORE_F64> {
   using T = double;
   using C = double;
   static __device__ __forceinline__ C load(T v) { return v; }
   static __device__ __forceinline__ T store(C v) { return v; }
-  static __device__ __forceinline__ C load(T v, float) { return v; }
-  static __device__ __forceinline__ T store(C v, float) { return v; }
 };
 template <>
 struct Store<LBM_STORE_F32> {
@@ -42,8 +34,6 @@ struct Store<LBM_STORE_F32> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return v; }
   static __device__ __forceinline__ T store(C v) { return v; }
-  static __device__ __forceinline__ C load(T v, float) { return v; }
-  static __device__ __forceinline__ T store(C v, float) { return v; }
 };
 template <>
 struct Store<LBM_STORE_F16_DEV> {
@@ -51,8 +41,6 @@ struct Store<LBM_STORE_F16_DEV> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return __half2float(v); }
   static __device__ __forceinline__ T store(C v) { return __float2half_rn(v); }
-  static __device__ __forceinline__ C load(T v, float k) { return __half2float(v) + k; }
-  static __device__ __forceinline__ T store(C v, float k) { return __float2half_rn(v - k); }
 };
 template <>
 struct Store<LBM_STORE_BF16_DEV> {
@@ -60,8 +48,6 @@ struct Store<LBM_STORE_BF16_DEV> {
   using C = float;
   static __device__ __forceinline__ C load(T v) { return __bfloat162float(v); }
   static __device__ __forceinline__ T store(C v) { return __float2bfloat16_rn(v); }
-  static __device__ __forceinline__ C load(T v, float k) { return __bfloat162float(v) + k; }
-  static __device__ __forceinline__ T store(C v, float k) { return __float2bfloat16_rn(v - k); }
 };
 
 // state value <-> population f of direction q
@@ -185,6 +171,150 @@ __device__ __forceinline__ void collide_ns(C om, bool force_in, const C* Fin, C*
       v[q] = fma(keep, v[q], E + O);
       v[o] = fma(keep, v[o], E - O);
     }
+  });
+}
+
+// Navier-Stokes BGK (+ Guo forcing) in single precision on the state shifted
+// to a free stream U along x (the dense-box engine's FP32 / FP16 / BF16
+// storages):
+//   s_q = v_q - S P_q(U),  P_q(u) = 3 c_q.u + 4.5 (c_q.u)^2 - 1.5 u^2,
+// the deviation of each population from the equilibrium at rho = 1 and u = U.
+// Every intermediate is a deviation from that free stream as well:
+//   r = rho - 1 = (sum w_q s_q) / S   (sum w_q P_q(U) = 0),
+//   du = u - U = (sum c_q w_q s_q / S + F/2 - r U) / rho,
+//   s_eq_q = S [r (1 - 1.5 U^2) - 1.5 rho du.(2U + du)]
+//            + 4.5 S [r (c_qx U)^2 + rho (c_q.du)(c_q.du + 2 c_qx U)]
+//            + 3 S [r c_qx U + rho c_q.du],
+// so in a flow near U the arithmetic rounds relative to small numbers.  (The
+// same update on v = s + S P(U) rounds relative to |v| ~ 600 in a flow at
+// U = 0.05, and over tens of thousands of steps that rounding acts like a
+// small body force.)  It is the BGK update itself: v' = (1 - omega) v +
+// omega v_eq maps to s' = (1 - omega) s + omega s_eq.  Opposite directions
+// share the even part (first two lines) and differ in the sign of the odd
+// part.  U = 0 gives the update on v.
+template <int LAT, bool FORCE = true>
+__device__ __forceinline__ void collide_ns_shifted(float om, bool force_in, const float* Fin, float U, float* sv, float* mom_out) {
+  const bool force = FORCE && force_in;
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  constexpr float S = static_cast<float>(STATE_SCALE), IS = static_cast<float>(1.0 / STATE_SCALE);
+  float           r0 = 0, j[3] = {0, 0, 0};
+  static_for<Q>([&](auto qc) {
+    constexpr int   q = decltype(qc)::value;
+    constexpr float w = static_cast<float>(L::w(q));
+    r0                = fmaf(w, sv[q], r0);
+    static_for<D>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      if constexpr(L::c(q, d) > 0) j[d] = fmaf(w, sv[q], j[d]);
+      if constexpr(L::c(q, d) < 0) j[d] = fmaf(-w, sv[q], j[d]);
+    });
+  });
+  const float r    = r0 * IS;
+  const float rho  = 1.0f + r;
+  const float irho = recip(rho);
+  float       F[3] = {0, 0, 0}, du[3] = {0, 0, 0};
+  if(force) static_for<D>([&](auto dc) { F[decltype(dc)::value] = Fin[decltype(dc)::value]; });
+  static_for<D>([&](auto dc) {
+    constexpr int d = decltype(dc)::value;
+    float         m = FORCE ? fmaf(j[d], IS, 0.5f * F[d]) : j[d] * IS;
+    if constexpr(d == 0) m = fmaf(-r, U, m);
+    du[d] = m * irho;
+  });
+  // du.(2U + du) = u^2 - U^2, and u.F
+  float dusq = du[0] * fmaf(2.0f, U, du[0]), uf = 0;
+  static_for<D>([&](auto dc) {
+    constexpr int d = decltype(dc)::value;
+    if constexpr(d > 0) dusq = fmaf(du[d], du[d], dusq);
+  });
+  if(force) {
+    uf = (U + du[0]) * F[0];
+    static_for<D>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      if constexpr(d > 0) uf = fmaf(du[d], F[d], uf);
+    });
+  }
+  if(mom_out) {
+    mom_out[0] = rho;
+    static_for<D>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      mom_out[1 + d]  = d == 0 ? U + du[0] : du[d];
+    });
+  }
+  const float keep = 1.0f - om;
+  const float oS   = om * S;
+  const float A    = oS * 4.5f * rho;
+  const float B    = oS * 3.0f * rho;
+  const float G    = S * (1.0f - 0.5f * om);  // Guo prefactor in state units
+  // the even constant part: rest and c_x = 0 directions, and c_x != 0 ones
+  float E0 = oS * fmaf(r, fmaf(-1.5f * U, U, 1.0f), -1.5f * rho * dusq);
+  if(force) E0 = fmaf(-3.0f * G, uf, E0);
+  const float E0x = fmaf(oS * 4.5f * r * U, U, E0);
+  const float Bu  = oS * 3.0f * r * U;
+  sv[Q - 1]       = fmaf(keep, sv[Q - 1], E0);
+  static_for<Q - 1>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    constexpr int o = L::opp(q);
+    if constexpr(q < o) {
+      // c_q.du and c_q.F, started from the first non-zero component (no 0 + x)
+      constexpr int d0  = L::c(q, 0) != 0 ? 0 : (L::c(q, 1) != 0 ? 1 : 2);
+      constexpr int cx  = L::c(q, 0);
+      float         cdu = L::c(q, d0) > 0 ? du[d0] : -du[d0];
+      float         cf  = L::c(q, d0) > 0 ? F[d0] : -F[d0];
+      static_for<D>([&](auto dc) {
+        constexpr int d = decltype(dc)::value;
+        if constexpr(d > d0 && L::c(q, d) > 0) {
+          cdu += du[d];
+          cf += F[d];
+        }
+        if constexpr(d > d0 && L::c(q, d) < 0) {
+          cdu -= du[d];
+          cf -= F[d];
+        }
+      });
+      float E, O;
+      if constexpr(cx == 0) {
+        E = fmaf(A * cdu, cdu, E0);
+        O = B * cdu;
+      } else {
+        const float tu = cx > 0 ? 2.0f * U : -2.0f * U;  // 2 c_qx U
+        E              = fmaf(A * cdu, cdu + tu, E0x);
+        O              = fmaf(B, cdu, cx > 0 ? Bu : -Bu);
+      }
+      if(force) {
+        const float cu = cx == 0 ? cdu : (cx > 0 ? cdu + U : cdu - U);
+        E              = fmaf(9.0f * G * cu, cf, E);
+        O              = fmaf(3.0f * G, cf, O);
+      }
+      sv[q] = fmaf(keep, sv[q], E + O);
+      sv[o] = fmaf(keep, sv[o], E - O);
+    }
+  });
+}
+
+// The shifted state of the equilibrium at (rho, u) in single precision (free
+// stream U along x): s_eq_q = v_eq_q - S P_q(U), the terms of
+// collide_ns_shifted with omega = 1.
+template <int LAT>
+__device__ __forceinline__ void equilibrium_shifted(float rho, const float* u, float U, float* out) {
+  using L         = Lattice<LAT>;
+  constexpr int Q = L::Q, D = L::D;
+  constexpr float S = static_cast<float>(STATE_SCALE);
+  const float     r = rho - 1.0f;
+  const float     du[3] = {u[0] - U, D > 1 ? u[1] : 0.0f, D > 2 ? u[2] : 0.0f};
+  const float     dusq  = fmaf(du[0], fmaf(2.0f, U, du[0]), fmaf(du[1], du[1], du[2] * du[2]));
+  const float     E0    = S * fmaf(r, fmaf(-1.5f * U, U, 1.0f), -1.5f * rho * dusq);
+  static_for<Q>([&](auto qc) {
+    constexpr int q   = decltype(qc)::value;
+    constexpr int cx  = L::c(q, 0);
+    float         cdu = 0;
+    static_for<D>([&](auto dc) {
+      constexpr int d = decltype(dc)::value;
+      if constexpr(L::c(q, d) != 0) cdu += static_cast<float>(L::c(q, d)) * du[d];
+    });
+    const float ux = static_cast<float>(cx) * U;
+    const float E  = E0 + S * 4.5f * fmaf(r * ux, ux, rho * cdu * (cdu + 2.0f * ux));
+    const float O  = S * 3.0f * fmaf(r, ux, rho * cdu);
+    out[q]         = E + O;
   });
 }
 
