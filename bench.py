@@ -69,8 +69,12 @@ def sphere_case(nx=512, ny=256, nz=256, radius=24.0, center=(128.0, 128.0, 128.0
     sub[inside] = 1
     flags[:, :, 0] = 2
     flags[:, :, -1] = 3
+    # started from the free stream (the equilibrium at rho = 1 and the inlet
+    # velocity in every fluid cell), the usual impulsive start of a flow past
+    # an obstacle
     return dict(shape=(nx, ny, nz), tau=tau, flags=flags.reshape(-1),
-                faces=("open", "open", "freeslip", "freeslip", "freeslip", "freeslip"), inlet=(0.05, 0.0, 0.0))
+                faces=("open", "open", "freeslip", "freeslip", "freeslip", "freeslip"), inlet=(0.05, 0.0, 0.0),
+                init=(0.05, 0.0, 0.0))
 
 
 class ClockSampler:
@@ -144,7 +148,7 @@ def cpu_baseline(threads: int, budget_s: float = 12.0):
     case = sphere_case(128, 64, 64, radius=6.0, center=(32.0, 32.0, 32.0))
     o = oracle.BoxOracle(D3Q19, case["shape"], 1.0 / case["tau"], faces=case["faces"], flags=case["flags"],
                          inlet_velocity=case["inlet"])
-    o.init_equilibrium()
+    o.init_equilibrium(1.0, case["init"])
     t0 = time.perf_counter()
     o.step(2, threads)
     dt = (time.perf_counter() - t0) / 2
@@ -182,11 +186,32 @@ def mass_drift(tau, device, steps=100_000):
     return out
 
 
+def long_horizon_accuracy(device, steps=5000):
+    """Velocity relative L2 of each storage against the plain FP64 method
+    after `steps` steps of the sphere case scaled to 256 x 128 x 128 (radius
+    12), all started from the free stream: the flow has passed the box twice."""
+    from lbm_gb300.solver import BoxSolver
+
+    case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
+    u = {}
+    for st in ("f64", "f32", "f16dev", "bf16dev"):
+        s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], st, faces=case["faces"], flags=case["flags"],
+                      inlet_velocity=case["inlet"], init_velocity=case["init"], device=device)
+        s.initial_condition()
+        s.step(steps)
+        u[st] = s.moments()[1]
+        s.close()
+    ref = u.pop("f64")
+    out = {st: float(np.linalg.norm(v - ref) / np.linalg.norm(ref)) for st, v in u.items()}
+    out["case"] = f"D3Q19 sphere 256x128x128 (r=12), {steps} steps from the free stream"
+    return out
+
+
 def run_variant(storage, case, warmup, steps, device):
     from lbm_gb300.solver import BoxSolver
 
     s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], storage, faces=case["faces"], flags=case["flags"],
-                  inlet_velocity=case["inlet"], device=device)
+                  inlet_velocity=case["inlet"], init_velocity=case["init"], device=device)
     s.initial_condition()
     s.step(warmup)
     s.synchronize()
@@ -423,7 +448,7 @@ def profile_case(args):
 
         case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
         s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
-                      inlet_velocity=case["inlet"])
+                      inlet_velocity=case["inlet"], init_velocity=case["init"])
         s.initial_condition()
         if args.kernel:
             s.kernel(args.kernel)
@@ -603,17 +628,22 @@ def main():
             del uu
     del u64
 
-    # mass conservation per storage (reported; a failure here never costs the line)
+    # mass conservation per storage and the error after a long run (reported;
+    # a failure here never costs the line)
     try:
         drift = mass_drift(case["tau"], device)
     except Exception as exc:
         drift = {"error": str(exc)[:200]}
+    try:
+        long_acc = long_horizon_accuracy(device)
+    except Exception as exc:
+        long_acc = {"error": str(exc)[:200]}
 
     # end to end through the C ABI with host buffers
     from lbm_gb300.solver import BoxSolver
 
     e = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.storage, faces=case["faces"], flags=case["flags"],
-                  inlet_velocity=case["inlet"], device=device)
+                  inlet_velocity=case["inlet"], init_velocity=case["init"], device=device)
     host = torch.empty((19, cells), dtype=torch.float64, pin_memory=True).numpy()
     w = np.array([1 / 18] * 6 + [1 / 36] * 12 + [1 / 3])
     host[:] = w[:, None]
@@ -663,6 +693,8 @@ def main():
                      "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},
         "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + 2 * args.steps,
+                     "start": "free stream (equilibrium at the inlet velocity)",
+                     "vel_rel_l2_vs_f64_long": long_acc,
                      "mass_drift_per_1e5_steps": drift,
                      "mass_drift_case": "closed D3Q19 sphere channel 96x64x64, periodic x, free-slip sides, u0 = 0.05"},
         "variants": variants,

@@ -496,8 +496,11 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
 
 // outlet ghost fill, run before every step: for each outlet cell and each
 // direction q with c_qx = -1, the population its upstream neighbour receives
+// skip_xface: the outlet cells of the inlet / outlet face rows (XFACE) read
+// their upstream cell from the row-staged kernel's shared memory instead
+// (box_rows.cu), so only the other outlet cells need a ghost value
 template <int LAT, int ST, bool ODD>
-__global__ void k_box_outlet(BoxParams P) {
+__global__ void k_box_outlet(BoxParams P, bool skip_xface) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -507,7 +510,8 @@ __global__ void k_box_outlet(BoxParams P) {
   if(y >= P.ny) return;
   const int     x  = P.nx - 1;
   const int64_t r  = x + static_cast<int64_t>(P.nx) * (y + static_cast<int64_t>(P.ny) * z);
-  if((P.flags[r] & TYPE_MASK) != LBM_CELL_OUTLET) return;
+  const uint8_t fl = P.flags[r];
+  if((fl & TYPE_MASK) != LBM_CELL_OUTLET || (skip_xface && (fl & XFACE))) return;
   T*            A  = static_cast<T*>(P.pop);
   const int64_t NA = P.nalloc;
   const int64_t u  = r - 1;
@@ -771,8 +775,12 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   const dim3 g   = step_grid(b, tpb);
   if(b->p.has_outlet) {
     const dim3 go(static_cast<unsigned>((b->p.ny + 127) / 128), static_cast<unsigned>(b->p.nz));
-    if(odd) k_box_outlet<LAT, ST, true><<<go, 128, 0, s>>>(b->p);
-    else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p);
+    // the row-staged kernel takes its outlet face cells' upstream values from
+    // its own staged rows (when the outlet and upstream cells share a warp)
+    const int  k    = odd ? b->kind_odd : b->kind_even;
+    const bool skip = k == LBM_BOX_KERNEL_ROWS && mom == 0 && box_rows_outlet_inline(b);
+    if(odd) k_box_outlet<LAT, ST, true><<<go, 128, 0, s>>>(b->p, skip);
+    else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p, skip);
   }
   if(ev0) cudaEventRecord(ev0, s);
   int64_t        nbulk = static_cast<int64_t>(g.x) * g.y * g.z * (tpb / 32);  // residual slots (warps) of the bulk kernel

@@ -111,6 +111,9 @@ cudaError_t box_tma_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t
 // qualifies, and the launch.  Its odd step must run before the boundary
 // kernel: it writes back the unchanged slots of the cells it does not step.
 bool        box_rows_supported(const BoxState* b);
+// whether the row-staged kernel reads its XFACE outlet cells' upstream
+// values from its staged rows (then the ghost fill skips those cells)
+bool        box_rows_outlet_inline(const BoxState* b);
 cudaError_t box_rows_bulk(BoxState* b, bool odd, cudaStream_t s);
 
 }  // namespace lbm

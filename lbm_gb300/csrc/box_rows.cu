@@ -97,12 +97,13 @@ struct RowList {
   int*     err;       // set to 1 when a wait times out
   uint64_t limit_ns;  // limit of each pipeline wait
   int      starve;    // test only: the producer never arms the CTA's first row, so the waits on it run out
+  int      outlet_inline;  // XFACE outlet cells read their upstream cell's values from the staged row
 };
 
 // One cell of a staged row.  bx: the cell's element in plane 0 of the stage
 // (index H + x).
 template <int LAT, int EQ, int ST, bool ODD, int WR>
-__device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z) {
+__device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z, bool outlet_inline) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -123,7 +124,8 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
   if(!work) return;
   // one vote per warp: warps of plain fluid cells take the path without the
   // inlet / outlet / Dirichlet branches
-  const bool any_special = __any_sync(__activemask(), special);
+  const unsigned active      = __activemask();
+  const bool     any_special = __any_sync(active, special);
   C          f[Q];
   if(!any_special) {
     static_for<Q>([&](auto qc) {
@@ -143,16 +145,30 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
         else f[q] = S::load(bx[q * WR]);
       });
       if(type == LBM_CELL_OUTLET) {
-        // links from beyond +x: what the upstream cell received (ghost plane)
-        const T*  A  = static_cast<const T*>(P.pop);
-        const int NA = static_cast<int>(P.nalloc);
-        static_for<Q>([&](auto qc) {
-          constexpr int q = decltype(qc)::value;
-          if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
-        });
+        if(outlet_inline && (flag & XFACE)) {
+          // links from beyond +x: what the upstream cell x - 1 receives, read
+          // from the staged row before that cell (the neighbouring lane)
+          // overwrites the slot (the warp syncs before its stores)
+          static_for<Q>([&](auto qc) {
+            constexpr int q = decltype(qc)::value;
+            if constexpr(L::c(q, 0) < 0) {
+              if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - 1 - L::c(q, 0)]);
+              else f[q] = S::load(bx[q * WR - 1]);
+            }
+          });
+        } else {
+          // links from beyond +x: what the upstream cell received (ghost plane)
+          const T*  A  = static_cast<const T*>(P.pop);
+          const int NA = static_cast<int>(P.nalloc);
+          static_for<Q>([&](auto qc) {
+            constexpr int q = decltype(qc)::value;
+            if constexpr(L::c(q, 0) < 0) f[q] = S::load(A[Q * NA + static_cast<int>(ghost_index(P, q, y, z))]);
+          });
+        }
       }
       collide<LAT, EQ, C>(P, f, nullptr);
     }
+    __syncwarp(active);  // every lane's staged reads come before any lane's stores
   }
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
@@ -280,7 +296,7 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
     }
     T* const stage = buf + st * STAGE + H;
 #pragma unroll 1
-    for(int x = tid; x < nx; x += kRowThreads) row_cell<LAT, EQ, ST, ODD, WR>(P, stage + x, x, y, z);
+    for(int x = tid; x < nx; x += kRowThreads) row_cell<LAT, EQ, ST, ODD, WR>(P, stage + x, x, y, z, R.outlet_inline != 0);
     fence_async_smem();  // this thread's writes are visible to the bulk stores
     __syncwarp();
     if(lane == 0) mbar_arrive(smem_u32(&done[st]));
@@ -344,6 +360,7 @@ cudaError_t launch_rows(BoxState* b, bool odd, cudaStream_t s) {
   R.err      = b->d_err;
   R.limit_ns = b->wait_limit_ns;
   R.starve   = b->wait_starve;
+  R.outlet_inline = box_rows_outlet_inline(b) ? 1 : 0;
   if(R.count == 0) return cudaSuccess;
   const int k = row_k(b->p.nx);
   if(k == 2) return odd ? launch_rows_one<LAT, EQ, ST, true, 2>(b, R, s) : launch_rows_one<LAT, EQ, ST, false, 2>(b, R, s);
@@ -360,6 +377,14 @@ size_t rows_smem_for(int nx) {
 }
 
 }  // namespace
+
+bool box_rows_outlet_inline(const BoxState* b) {
+  // the outlet cell x = nx - 1 and its upstream cell x - 1 are stepped by two
+  // lanes of one warp in the same pass over the row (cells x and x +
+  // kRowThreads k per thread, 32 consecutive cells per warp)
+  const int x = b->p.nx - 1;
+  return b->p.has_outlet && x % 32 != 0;
+}
 
 bool box_rows_supported(const BoxState* b) {
   // every staged row starts on a 16-byte boundary (planes are padded to 128
