@@ -446,7 +446,10 @@ def profile_case(args):
     if args.profile_case in B_PER_CELL:
         from lbm_gb300.solver import BoxSolver
 
-        case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
+        if args.profile_size == "slab":
+            case = sphere_case(512, 256, 64, radius=24.0, center=(128.0, 128.0, 32.0))
+        else:
+            case = sphere_case(256, 128, 128, radius=12.0, center=(64.0, 64.0, 64.0))
         s = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], args.profile_case, faces=case["faces"], flags=case["flags"],
                       inlet_velocity=case["inlet"], init_velocity=case["init"])
         s.initial_condition()
@@ -531,6 +534,9 @@ def main():
                          "(batch 8, 128x512)")
     ap.add_argument("--kernel", default=None, choices=["thread", "staged", "paired", "rows"],
                     help="--profile-case: force this bulk kernel")
+    ap.add_argument("--profile-size", default="small", choices=["small", "slab"],
+                    help="--profile-case of the sphere: 256x128x128 (r=12), or a 512x256x64 slab of the full box (r=24): "
+                         "full-length rows, state well above L2")
     args = ap.parse_args()
     if args.profile_case:
         print(json.dumps(profile_case(args)))
@@ -690,7 +696,8 @@ def main():
                      "traffic": PROFILED_TRAFFIC_PER_STEP.get(args.storage),
                      "traffic_source": "ncu capture of this workload's step kernels (dram__bytes_read.sum + dram__bytes_write.sum "
                                        "per step), recorded with the source; not measured in this run", "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
-                     "peak_kind": peak_kind, "kernel": "AA step (k_box_tma or k_box_bulk, + k_box_bnd, k_box_outlet)",
+                     "peak_kind": peak_kind, "kernel": "AA step (the bulk kernel the autotuner picked: k_box_rows, k_box_bulk_lean or k_box_tma; + k_box_bnd, "
+                               "k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},
         "accuracy": {"vel_rel_l2_vs_f64": err_head, "after_steps": args.warmup + 2 * args.steps,
                      "start": "free stream (equilibrium at the inlet velocity)",
