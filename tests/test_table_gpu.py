@@ -108,8 +108,9 @@ def test_reference_analytic_suite(name):
     reference's number of steps (at convergence, or at maxSteps where the
     reference does not converge either), passes the reference's bounds
     (compareToAnalyticalResult, src/lbm/solver.cpp:387-482), and reports the
-    reference's own max / L2 / GRE errors to 1e-10 relative (the values the
-    reference's run() printed, tests/golden/analytic_suite.json)."""
+    reference's own max / L2 / GRE errors (the values the reference's run()
+    printed, tests/golden/analytic_suite.json) to 1e-10 relative or 1e-14
+    absolute."""
     from lbm_gb300.solver import LBMSolver
 
     e = _analytic_cases()[name]
@@ -120,11 +121,15 @@ def test_reference_analytic_suite(name):
     assert res["steps"] == e["steps"], (res["steps"], e["steps"])
     cmp = s.compare_to_analytical()
     assert cmp["passed"], cmp
+    # 1e-10 relative; where the errors themselves sit at the rounding level of
+    # the velocities (the converged Couette cases, max error ~1e-12 on
+    # velocities of ~0.1) the last bits of the analytic profile decide them,
+    # and 1e-14 absolute is the bar
     for k in ("max", "l2", "gre"):
         ref = e[k]
         if ref is None:
             continue
-        assert abs(cmp[k] - ref) <= 1e-10 * abs(ref), (k, cmp[k], ref)
+        assert abs(cmp[k] - ref) <= max(1e-10 * abs(ref), 1e-14), (k, cmp[k], ref)
 
 
 @pytest.mark.parametrize("name", ["cavity_small_100", "poisson2d_helmholtz_small_100"])
