@@ -258,8 +258,11 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
 // per thread: the step is bound by memory latency and instruction issue
 // together, and the extra resident warps hide more of the latency than the
 // compiler's own register choice (48-64 on D3Q19) does.
+#ifndef LBM_LEAN_REGS
+#define LBM_LEAN_REGS 40
+#endif
 template <int LAT, int EQ, int ST, bool ODD>
-__global__ void __maxnreg__(40) k_box_bulk_lean(BoxParams P) {
+__global__ void __maxnreg__(LBM_LEAN_REGS) k_box_bulk_lean(BoxParams P) {
   bulk_grid_cell<LAT, EQ, ST, ODD, 0>(P);
 }
 
