@@ -41,10 +41,11 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 D3Q19 = 4
 B_PER_CELL = {"f64": 2 * 19 * 8 + 1, "f32": 2 * 19 * 4 + 1, "f16dev": 2 * 19 * 2 + 1, "bf16dev": 2 * 19 * 2 + 1}
 METRIC = "MLUPS (D3Q19 sphere 512x256x256, FP16-deviation storage)"
-# DRAM bytes (read + write) per step of this workload, averaged over the two
-# step parities (bulk + boundary + outlet kernels): taken from an ncu capture
-# of this workload's step kernels, not measured by this script
-PROFILED_TRAFFIC_PER_STEP = {"f16dev": 2.58e9}
+# DRAM bytes (read + write) per launch of the bulk step kernel on this
+# workload, averaged over the two step parities: taken from an ncu capture on
+# the 512x256x64 slab of the sphere case and scaled by cells to the full box;
+# not measured by this script
+PROFILED_TRAFFIC_PER_STEP = {"f16dev": 2.32e9}
 
 
 def peaks():
@@ -204,6 +205,46 @@ def long_horizon_accuracy(device, steps=5000):
     ref = u.pop("f64")
     out = {st: float(np.linalg.norm(v - ref) / np.linalg.norm(ref)) for st, v in u.items()}
     out["case"] = f"D3Q19 sphere 256x128x128 (r=12), {steps} steps from the free stream"
+    return out
+
+
+def accuracy_run(args):
+    """Velocity relative L2 against the plain FP64 method of every storage,
+    with and without the free-stream shift of the single-precision state,
+    at checkpoints of a long run of the sphere case: the 256x128x128 sample
+    (r=12) to 50,000 steps and the full 512x256x256 box to 10,000 steps, both
+    started from the free stream."""
+    from lbm_gb300.solver import BoxSolver
+
+    out = {"metric": "velocity relative L2 vs FP64 (D3Q19 sphere)", "unit": "relative L2", "higher_is_better": False,
+           "dtype": "f64 reference; f32 / f16 / bf16 storage with f32 arithmetic", "data": "synthetic", "rows": []}
+    spec = {"f64": ("f64", True), "f32": ("f32", True), "f32_noshift": ("f32", False), "f16dev": ("f16dev", True),
+            "f16dev_noshift": ("f16dev", False), "bf16dev": ("bf16dev", True)}
+    for (nx, ny, nz, r, c), checkpoints in (((256, 128, 128, 12.0, (64.0, 64.0, 64.0)), (1000, 5000, 20000, 50000)),
+                                           ((512, 256, 256, 24.0, (128.0, 128.0, 128.0)), (2000, 5000, 10000))):
+        case = sphere_case(nx, ny, nz, radius=r, center=c)
+        sol = {}
+        for n, (st, sh) in spec.items():
+            sol[n] = BoxSolver(D3Q19, case["shape"], 1.0 / case["tau"], st, faces=case["faces"], flags=case["flags"],
+                               inlet_velocity=case["inlet"], init_velocity=case["init"], shift=sh)
+            sol[n].initial_condition()
+        done = 0
+        for cp in checkpoints:
+            for sv in sol.values():
+                sv.step(cp - done)
+            done = cp
+            u64 = sol["f64"].moments()[1]
+            row = {"case": f"{nx}x{ny}x{nz}", "steps": cp}
+            for n, sv in sol.items():
+                if n != "f64":
+                    row[n] = float(np.linalg.norm(sv.moments()[1] - u64) / np.linalg.norm(u64))
+            out["rows"].append(row)
+            print(json.dumps(row), file=sys.stderr, flush=True)
+        for sv in sol.values():
+            sv.close()
+    out["value"] = next(r["f16dev"] for r in out["rows"] if r["case"] == "512x256x256" and r["steps"] == 5000)
+    out["config"] = {"workload": "D3Q19 flow past a sphere from the free stream; value: FP16 storage, full box, 5,000 steps",
+                     "tau": sphere_case(64, 32, 32)["tau"]}
     return out
 
 
@@ -518,7 +559,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt"],
+    ap.add_argument("--workload", default="sphere",
+                    choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt", "accuracy"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
@@ -558,7 +600,7 @@ def main():
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
-                  "grid": grid_run, "lpt": lpt_run}[args.workload]
+                  "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run}[args.workload]
             print(json.dumps(fn(args)))
         return
 
@@ -694,8 +736,9 @@ def main():
                    "bulk_kernel": bulk_kernel},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": PROFILED_TRAFFIC_PER_STEP.get(args.storage),
-                     "traffic_source": "ncu capture of this workload's step kernels (dram__bytes_read.sum + dram__bytes_write.sum "
-                                       "per step), recorded with the source; not measured in this run", "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
+                     "traffic_source": "ncu capture of the bulk step kernel (dram__bytes_read.sum + dram__bytes_write.sum) on the "
+                                       "512x256x64 slab of this workload, scaled by cells to the full box; recorded with the source, "
+                                       "not measured in this run", "algorithmic_bytes": B_PER_CELL[args.storage] * cells,
                      "peak_kind": peak_kind, "kernel": "AA step (the bulk kernel the autotuner picked: k_box_rows, k_box_bulk_lean or k_box_tma; + k_box_bnd, "
                                "k_box_outlet)",
                      "kernel_avg_ms": kernel_avg_ms},

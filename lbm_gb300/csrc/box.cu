@@ -254,12 +254,14 @@ __global__ void __launch_bounds__(256) k_box_bulk(BoxParams P) {
   bulk_grid_cell<LAT, EQ, ST, ODD, MOM>(P);
 }
 
-// The plain step of the FP32 / FP16 / BF16 storages with at most 40 registers
+// The plain step of the FP32 / FP16 / BF16 storages with at most 48 registers
 // per thread: the step is bound by memory latency and instruction issue
 // together, and the extra resident warps hide more of the latency than the
-// compiler's own register choice (48-64 on D3Q19) does.
+// compiler's own register choice (64-72 on D3Q19) does.  40 registers spill
+// the free-stream-shifted collision; 48 and 64 time alike on the 512x256x256
+// sphere, 56 is slower.
 #ifndef LBM_LEAN_REGS
-#define LBM_LEAN_REGS 40
+#define LBM_LEAN_REGS 48
 #endif
 template <int LAT, int EQ, int ST, bool ODD>
 __global__ void __maxnreg__(LBM_LEAN_REGS) k_box_bulk_lean(BoxParams P) {
