@@ -15,7 +15,8 @@
  * padding 1, with cin and cout multiples of 32.  `ld*` is the channel stride
  * of a tensor (>= its channel count) and `off*` a channel offset into it, so
  * concatenations are views.  `stream` is a cudaStream_t.  Return 0 on success,
- * -1 for invalid arguments, -2 for a CUDA launch error.
+ * -1 for invalid arguments, -2 for a CUDA launch error, -6 (lbm_nn_conv_status
+ * only) for a bounded device wait that ran out.
  */
 #ifndef LBM_UNET_H
 #define LBM_UNET_H
@@ -26,7 +27,10 @@
 extern "C" {
 #endif
 
-/* y[:, offy:offy+cout] = act(conv(x[:, :cin], w) + bias); out_f32 selects FP32 output */
+/* y[:, offy:offy+cout] = act(conv(x[:, :cin], w) + bias); out_f32 selects FP32 output.  Runs on the tcgen05
+ * tensor-core kernel where the shape qualifies (cout <= 256; W a multiple of 128, or a divisor of 128 with
+ * H a multiple of 128 / W; x, w, y 16-byte aligned; ldy, offy multiples of 8 for BF16 output, of 4 for FP32),
+ * else on the mma.sync kernel */
 int lbm_nn_conv3x3_fwd(const void* x, int ldx, const void* w, const float* bias, void* y, int ldy, int offy, int B, int H, int W, int cin,
                        int cout, int relu, int out_f32, void* stream);
 /* dw [cout][9 cin] = sum over pixels of dy (x) shifted x; partial: FP32 scratch of partial_floats */
@@ -53,6 +57,14 @@ int lbm_nn_mse(const float* pred, int ldp, const float* target, const uint8_t* f
 int lbm_nn_adam(float* w, void* w16, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps, int step,
                 void* stream);
 int lbm_nn_to_bf16(const float* a, void* b, int64_t n, void* stream);
+/* 0: the tensor-core convolution where it qualifies (default); 1: the mma.sync kernel only */
+int lbm_nn_set_conv_path(int path);
+/* 1 if lbm_nn_conv3x3_fwd with these arguments runs on the tensor-core kernel, else 0 */
+int lbm_nn_conv_uses_tc(const void* x, int ldx, const void* w, const void* y, int ldy, int offy, int B, int H, int W, int cin, int cout,
+                        int out_f32);
+/* synchronises the stream; -6 (a bounded pipeline wait of a tensor-core convolution ran out since the last
+ * call) or 0, and clears the flag */
+int lbm_nn_conv_status(void* stream);
 
 #ifdef __cplusplus
 }

@@ -34,6 +34,7 @@ UNITS = {
     "noalloc.cu": [],
     "batch.cu": [],
     "unet.cu": [],
+    "conv_tc.cu": [],
     # host-only grid and table build: no floating-point contraction, so that
     # the cut tests round as the reference's do on either host architecture
     "grid.cpp": ["-Xcompiler", "-ffp-contract=off"],

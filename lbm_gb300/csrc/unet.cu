@@ -400,11 +400,21 @@ int status(cudaError_t e) { return e == cudaSuccess ? 0 : -2; }
 
 }  // namespace
 
+namespace lbm {
+bool conv_tc_qualifies(const void* x, int ldx, const void* w, const void* y, int ldy, int offy, int B, int H, int W, int cin, int cout,
+                       int out_f32);
+int  conv_tc_launch(const void* x, int ldx, const void* w, const float* bias, void* y, int ldy, int offy, int B, int H, int W, int cin,
+                    int cout, int relu, int out_f32, cudaStream_t s);
+}  // namespace lbm
+
 extern "C" {
 
 int lbm_nn_conv3x3_fwd(const void* x, int ldx, const void* w, const float* bias, void* y, int ldy, int offy, int B, int H, int W, int cin,
                        int cout, int relu, int out_f32, void* stream) {
   if(cin % 32 || cout % 32 || ldx % 8 || ldx < cin || (!out_f32 && ldy % 2) || offy % 2 || B <= 0 || H <= 0 || W <= 0) return -1;
+  // the tcgen05 kernel (conv_tc.cu) where the shape and alignment qualify
+  if(lbm::conv_tc_qualifies(x, ldx, w, y, ldy, offy, B, H, W, cin, cout, out_f32))
+    return lbm::conv_tc_launch(x, ldx, w, bias, y, ldy, offy, B, H, W, cin, cout, relu, out_f32, static_cast<cudaStream_t>(stream));
   ConvFwd a{static_cast<const bf16*>(x), ldx, static_cast<const bf16*>(w), bias, y, ldy, offy, B, H, W, cin, cout};
   const int64_t P = static_cast<int64_t>(B) * H * W;
   dim3          grid(static_cast<unsigned>((P + BM - 1) / BM), static_cast<unsigned>((cout + BN - 1) / BN));

@@ -55,6 +55,10 @@ _NN = {
     "lbm_nn_adam": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float,
                     C.c_int, C.c_void_p],
     "lbm_nn_to_bf16": [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p],
+    "lbm_nn_set_conv_path": [C.c_int],
+    "lbm_nn_conv_uses_tc": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                            C.c_int],
+    "lbm_nn_conv_status": [C.c_void_p],
 }
 
 
@@ -297,7 +301,9 @@ class UNet:
         _ck(self.lib.lbm_nn_mse(self.a["out"].data_ptr(), 32, self.target.data_ptr(), self.fluid.data_ptr(), npix, self.NOUT, 1.0 / count,
                                 self.g["out"].data_ptr(), self.loss_part.data_ptr(), nb, self.stream), "mse")
         self.backward()
-        return float(self.loss_part[:nb].double().sum().item()) / count
+        loss = float(self.loss_part[:nb].double().sum().item()) / count
+        _ck(self.lib.lbm_nn_conv_status(self.stream), "tensor-core convolution (a pipeline wait ran out)")
+        return loss
 
     def adam(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8):
         self.step_count += 1
@@ -307,7 +313,9 @@ class UNet:
     def predict(self, x: np.ndarray) -> np.ndarray:
         """(B, H, W, 3) FP32 prediction for input channels x."""
         out = self.forward(x)
-        return out[..., : self.NOUT].float().cpu().numpy()
+        pred = out[..., : self.NOUT].float().cpu().numpy()
+        _ck(self.lib.lbm_nn_conv_status(self.stream), "tensor-core convolution (a pipeline wait ran out)")
+        return pred
 
     def get_params(self) -> np.ndarray:
         return self.w32.cpu().numpy()
