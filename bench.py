@@ -601,7 +601,11 @@ def main():
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
                   "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run}[args.workload]
-            print(json.dumps(fn(args)))
+            # clocks sampled over the whole workload run (set-up included)
+            with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+                line = fn(args)
+            line["clocks"] = clk.summary()
+            print(json.dumps(line))
         return
 
     rank = int(os.environ.get("RANK", "0"))

@@ -193,6 +193,39 @@ def test_reduced_precision_storage_against_fp64(storage, bound):
     assert err <= bound
 
 
+# velocity relative L2 against FP64 after 5,000 steps of the 256x128x128
+# sphere from the free stream, as measured on a GB300 by
+# `bench.py --workload accuracy`; the bound is twice that
+LONG_HORIZON_MEASURED = {"f32": 1.571e-6, "f16dev": 3.321e-5, "bf16dev": 7.209e-4}
+
+
+@pytest.mark.parametrize("storage", sorted(LONG_HORIZON_MEASURED))
+def test_reduced_precision_storage_long_horizon(storage):
+    """The headline flow past a sphere (D3Q19, equilibrium inlet u = 0.05,
+    zero-gradient outlet, free-slip sides, tau of the seed) on its 256x128x128
+    sample (r = 12), started from the free stream: after 5,000 steps the
+    velocity of each single-precision storage is within twice its measured
+    distance from the plain FP64 method.  The distance is the storage's
+    rounding floor: FP16 keeps 11 significant bits of the free-stream-shifted
+    state, BF16 8, FP32 24."""
+    from lbm_gb300 import cases
+    from lbm_gb300.solver import BoxSolver
+
+    c = cases.sphere_channel(nx=256, ny=128, nz=128, radius=12.0, center=(64.0, 64.0, 64.0))
+    kw = cases.box_kwargs(c)
+    sol = {}
+    for st in ("f64", storage):
+        sol[st] = BoxSolver(c["lattice"], c["shape"], c["omega"], st, init_velocity=(0.05, 0.0, 0.0), **kw)
+        sol[st].initial_condition()
+        sol[st].step(5000)
+    u64 = sol["f64"].moments()[1]
+    err = rel_l2(sol[storage].moments()[1], u64)
+    print(f"{storage}: velocity relative L2 vs FP64 after 5,000 steps = {err:.3e}")
+    assert err <= 2.0 * LONG_HORIZON_MEASURED[storage]
+    for sv in sol.values():
+        sv.close()
+
+
 def test_mass_conservation_closed_box():
     g, _ = make_pair("d3q19_lid")
     g.initial_condition()
