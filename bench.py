@@ -267,7 +267,8 @@ def run_variant(storage, case, warmup, steps, device):
 def cavities_run(args, dist=None):
     """The batched cavities (2048 D2Q9 lid-driven cavities, sides 32-512,
     Re 10-1000, FP32): device-timed steps of the whole batch, then a bounded
-    run with the convergence check (residual 1e-8, every 100 steps).  Under
+    run with the convergence check (residual 1e-8, every 100 steps), and (one
+    GPU) the FP32 error at convergence on a subset run in FP64 too.  Under
     torchrun every rank takes a contiguous share of the cavities balanced by
     cells (lbm_gb300.shard) and steps it on its own GPU; the job time is the
     slowest rank's and the per-cavity results are gathered on every rank."""
@@ -324,14 +325,59 @@ def cavities_run(args, dist=None):
                          "kernel_avg_ms": kernel_avg_ms},
             "run": {"max_steps": args.cavity_steps, "wall_s": wall, "mlups": updates / wall / 1e6,
                     "converged": int(np.sum(status == BatchSolver.CONVERGED)), "diverged": int(np.sum(status == BatchSolver.DIVERGED)),
-                    "of": int(len(area_all)), "final_residual_min_median_p90_max": res_q}}
+                    "of": int(len(area_all)), "final_residual_min_median_p90_max": res_q},
+            **({"f32_vs_f64_at_convergence": cavities_against_fp64(c)} if world == 1 and args.cavity_check else {})}
+
+
+def cavities_against_fp64(c, max_steps: int = 100000, count: int = 48):
+    """The FP32 batch's stated error at convergence: up to `count` of the
+    cavities whose slowest viscous mode decays within the configuration's step
+    bound (10 n Re <= 1e5, i.e. n^2 / nu <= 1e5 at lid speed 0.1), run to
+    residual 1e-8 (every 100 steps, at most `max_steps`) in FP64 and in FP32
+    storage; per cavity, the velocity relative L2 of the FP32 state against
+    the converged FP64 one."""
+    from lbm_gb300.solver import BatchSolver
+    from lbm_gb300.warmstart import C_D2Q9
+
+    sides, re = c["sides"], c["re"]
+    pick = np.flatnonzero(10.0 * sides * re <= 1e5)
+    pick = pick[np.linspace(0, len(pick) - 1, min(count, len(pick))).astype(int)] if len(pick) else pick
+    out = {"cavities": int(len(pick)), "selection": "10 n Re <= 1e5, evenly spaced over the batch", "max_steps": max_steps}
+    if not len(pick):
+        return out
+    res = {}
+    for st in ("f64", "f32"):
+        b = BatchSolver(sides[pick], 1.0 / c["tau"][pick], c["lid"], st)
+        b.initial_condition()
+        t0 = time.perf_counter()
+        steps = b.run(max_steps, 100, 1e-8, raise_on_divergence=False)
+        wall = time.perf_counter() - t0
+        u = []
+        for d in range(len(pick)):
+            f = b.domain_populations(d)
+            rho = f.sum(axis=0)
+            u.append(np.stack([(C_D2Q9[:, k, None] * f).sum(axis=0) / rho for k in range(2)]))
+        res[st] = dict(steps=steps, status=b.status(), u=u, wall=wall, resid=b.residuals().max(axis=1))
+        b.close()
+    conv64 = res["f64"]["status"] == BatchSolver.CONVERGED
+    err = np.array([np.linalg.norm(a - b) / np.linalg.norm(b) for a, b in zip(res["f32"]["u"], res["f64"]["u"])])
+    q = lambda v: [float(x) for x in np.percentile(v, [0, 50, 100])] if len(v) else None  # noqa: E731
+    out.update({"f64_converged": int(conv64.sum()), "f64_steps_min_median_max": q(res["f64"]["steps"][conv64]),
+                "f64_wall_s": res["f64"]["wall"], "f32_converged": int(np.sum(res["f32"]["status"] == BatchSolver.CONVERGED)),
+                "f32_final_residual_min_median_max": q(res["f32"]["resid"]),
+                "f32_vel_rel_l2_vs_f64_min_median_max": q(err[conv64]),
+                "sides_min_max": [int(sides[pick].min()), int(sides[pick].max())],
+                "re_min_max": [float(re[pick].min()), float(re[pick].max())]})
+    return out
 
 
 def poisson_run(args):
     """D3Q7 Poisson-Boltzmann on 256^3 (seeded charged spheres, Debye length
     and surface potentials by seed): device-timed steps in FP32 storage, the
-    FP32 solve to residual 1e-10 (FP64 residual reductions), and the FP32
-    potential against an FP64 run after the same 5,000 steps."""
+    FP32 solve to residual 1e-10 (FP64 residual reductions), the FP32
+    potential against an FP64 run after the same 5,000 steps, and the FP32
+    end state against the FP64 solve to the same residual (at most 100,000
+    steps)."""
     from lbm_gb300 import cases
     from lbm_gb300.solver import BoxSolver
 
@@ -356,6 +402,7 @@ def poisson_run(args):
     steps, res = g.run_to(1e-10, 1000, args.max_steps - 5000)
     wall = time.perf_counter() - t0
     out["solve_f32"] = {"steps": steps + 5000, "wall_s_after_5000": wall, "residual": float(np.max(res)), "converged": bool(np.max(res) < 1e-10)}
+    phi32_end, _ = g.moments()
     g.close()
     h = BoxSolver(c["lattice"], c["shape"], c["omega"], "f64", pb_nonlinear=True, **kw)
     h.initial_condition()
@@ -363,9 +410,64 @@ def poisson_run(args):
     h.step(5000)
     out["f64_mlups"] = cells * 5000 / (time.perf_counter() - t0) / 1e6
     phi64, _ = h.moments()
-    h.close()
     out["phi_rel_l2_f32_vs_f64_at_5000"] = float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64))
+    # the FP64 solve to the configuration's residual, and the FP32 end state's
+    # stated error against it
+    t0 = time.perf_counter()
+    steps64, res64 = h.run_to(1e-10, 1000, min(args.max_steps, 100000) - 5000)
+    phi64_end, _ = h.moments()
+    h.close()
+    out["solve_f64"] = {"steps": steps64 + 5000, "wall_s_after_5000": time.perf_counter() - t0, "residual": float(np.max(res64)),
+                        "converged": bool(np.max(res64) < 1e-10)}
+    out["phi_rel_l2_f32_end_vs_f64_converged"] = float(np.linalg.norm(phi32_end - phi64_end) / np.linalg.norm(phi64_end))
     return out
+
+
+def sweep_run(args):
+    """A sweep over geometry and Reynolds number stepped by one launch per
+    step: 256 inlet-driven D2Q9 channels 512x128 (1-8 cylinders each, Re
+    20-200 by seed, inlet u = 0.05) as the z-slices of one box, each slice
+    relaxing at its own rate, FP32 storage.  Device-timed steps and the HBM
+    fraction; then three slices checked bit for bit against boxes of their
+    own after 100 steps."""
+    from lbm_gb300 import cases
+    from lbm_gb300.solver import BoxSolver
+
+    n_ch, nx, ny = 256, 512, 128
+    chans = [cases.cylinder_channel(s, nx=nx, ny=ny) for s in range(n_ch)]
+    st = cases.stacked_sweep(chans)
+    g = BoxSolver(st["lattice"], st["shape"], st["omega"], "f32", **cases.box_kwargs(st))
+    g.set_slice_omega(st["slice_omega"])
+    g.initial_condition()
+    g.step(args.warmup)
+    tot, ker, n = g.profile_steps(args.steps)
+    cells = nx * ny * n_ch
+    bpc = 2 * 9 * 4 + 1
+    hbm, peak_kind = peaks()
+    ach = bpc * cells / (ker / n / 1e3) / 1e9
+    g.initial_condition()
+    g.step(100)
+    f = g.populations()
+    same = {}
+    for k in (0, n_ch // 2, n_ch - 1):
+        one = cases.stacked_sweep([chans[k]])
+        s1 = BoxSolver(one["lattice"], one["shape"], 1.0 / chans[k]["tau"], "f32", **cases.box_kwargs(one))
+        s1.initial_condition()
+        s1.step(100)
+        same[str(k)] = bool(np.array_equal(f[:, k * nx * ny:(k + 1) * nx * ny], s1.populations()))
+        s1.close()
+    kernel = g.kernel()
+    g.close()
+    re = [c["re"] for c in chans]
+    return {"metric": "MLUPS (sweep: 256 D2Q9 cylinder channels 512x128, Re 20-200, FP32, one launch per step)",
+            "value": cells * args.steps / (tot / 1e3) / 1e6, "unit": "MLUPS", "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot / args.steps, "dtype": "f32", "higher_is_better": True,
+            "config": {"workload": "256 inlet-driven D2Q9 channels 512x128 with 1-8 cylinders, Re 20-200 by seed, one relaxation "
+                                   "rate per slice", "cells": cells, "bytes_per_cell": bpc, "re_min_max": [min(re), max(re)],
+                       "bulk_kernel": kernel},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_kind": peak_kind,
+                         "kernel_avg_ms": ker / n},
+            "slices_bitwise_vs_own_boxes_after_100_steps": same}
 
 
 def poiseuille_run(args):
@@ -560,7 +662,7 @@ def main():
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
     ap.add_argument("--workload", default="sphere",
-                    choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt", "accuracy"],
+                    choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt", "accuracy", "sweep"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
@@ -569,6 +671,7 @@ def main():
     ap.add_argument("--ws-per-batch", type=int, default=32, help="warm start: training channels per Reynolds number")
     ap.add_argument("--ws-lr", type=float, default=1e-3, help="warm start: peak learning rate")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
+    ap.add_argument("--cavity-check", type=int, default=1, help="cavities: also run a subset to convergence in FP64 and FP32 (1) or not (0)")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL) + ["cavities", "poisson", "unet"],
                     help="a small case for ncu captures, its measured launches inside the NVTX range 'profile': 4 steps of "
                          "a 256x128x128 version of the sphere workload in this storage; or 4 steps of 256 of the cavities; "
@@ -600,7 +703,7 @@ def main():
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
-                  "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run}[args.workload]
+                  "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run, "sweep": sweep_run}[args.workload]
             # clocks sampled over the whole workload run (set-up included)
             with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
                 line = fn(args)

@@ -127,6 +127,15 @@ int lbm_gpu_box_select_kernel(lbm_gpu_ctx* ctx, int32_t kernel, int32_t* selecte
  * (lbm_gpu_box_select_kernel sets both, and reports -1 when they differ). */
 int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd);
 
+/* Navier-Stokes boxes: a relaxation rate per z-slice (omega[z], 0 < omega < 2,
+ * n = nz values), so that the independent 2D slices of a D2Q9 box are a
+ * sweep over Reynolds number (and geometry) stepped by one launch per step;
+ * omega = NULL restores the box's single rate.  Every slice then steps
+ * exactly as a box of its own with that rate.  The reference builds one
+ * solver per configuration (src/lbm/solverExe.h:17-93); this has no
+ * counterpart there.  LBM_ERR_UNSUPPORTED for Poisson boxes. */
+int lbm_gpu_box_set_slice_omega(lbm_gpu_ctx* ctx, const double* omega, int32_t n);
+
 /* TEST ONLY.  The staged kernels' (LBM_BOX_KERNEL_STAGED and
  * LBM_BOX_KERNEL_ROWS) pipeline waits are bounded (0.5 s each);
  * when one runs out the kernel records a flag, lets its copies in flight

@@ -158,6 +158,22 @@ def stacked_channels(cases_: List[Dict], tau: float) -> Dict:
                 faces=("open", "open", "wall", "wall", "periodic", "periodic"), inlet_velocity=(cases_[0]["u_in"], 0.0, 0.0))
 
 
+def stacked_sweep(cases_: List[Dict]) -> Dict:
+    """Inlet-driven channels (cylinder_channel) of any Reynolds numbers as the
+    z-slices of one D2Q9 box: a sweep over geometry and Re stepped together,
+    each slice relaxing at its own rate (`slice_omega`, for
+    BoxSolver.set_slice_omega).  All channels share the box shape and the
+    inlet speed."""
+    nx, ny = cases_[0]["shape"]
+    u_in = cases_[0]["u_in"]
+    if any(tuple(c["shape"]) != (nx, ny) or c["u_in"] != u_in for c in cases_):
+        raise ValueError("the channels of a sweep share the shape and the inlet speed")
+    flags = np.stack([c["flags"] for c in cases_]).reshape(-1)
+    return dict(lattice=D2Q9, shape=(nx, ny, len(cases_)), omega=1.0 / cases_[0]["tau"], flags=flags,
+                faces=("open", "open", "wall", "wall", "periodic", "periodic"), inlet_velocity=(u_in, 0.0, 0.0),
+                slice_omega=[1.0 / c["tau"] for c in cases_])
+
+
 def box_kwargs(case: Dict) -> Dict:
     """The BoxSolver / BoxOracle keyword arguments of a case."""
     keys = ("faces", "flags", "wall_velocity", "body_force", "inlet_velocity", "equation", "kappa_sq", "dirichlet")

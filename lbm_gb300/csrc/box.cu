@@ -125,7 +125,7 @@ __device__ __forceinline__ void bulk_finish(const BoxParams& P, int y, int z, in
         });
       }
     }
-    collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
+    collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
   }
   moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
   if constexpr(!ODD) {
@@ -351,8 +351,8 @@ __global__ void __launch_bounds__(256) k_box_pair(BoxParams P) {
       }
     }
   });
-  collide<LAT, EQ, C>(P, f0, nullptr);
-  collide<LAT, EQ, C>(P, f1, nullptr);
+  collide<LAT, EQ, C>(P, z, f0, nullptr);
+  collide<LAT, EQ, C>(P, z, f1, nullptr);
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     if constexpr(!ODD) {
@@ -486,7 +486,8 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
         f[q]            = S::load(A[src[q * n + i]]);
         if(corr_src) f[q] += static_cast<C>(corr_src[q * n + i]);
       });
-      collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
+      const int z = P.slice_omega ? static_cast<int>(cell / (static_cast<int64_t>(P.nx) * P.ny)) : 0;
+      collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
     }
     if(corr_dst)
       static_for<Q>([&](auto qc) { f[decltype(qc)::value] += static_cast<C>(corr_dst[decltype(qc)::value * n + i]); });
@@ -1123,6 +1124,8 @@ void box_destroy(BoxState* b) {
   cudaFree(b->pop_alloc);
   cudaFree(b->flags);
   cudaFree(b->dirichlet);
+  cudaFree(b->slice_omega);
+  cudaFree(b->slice_omega_f);
   cudaFree(b->mom);
   cudaFree(b->partials);
   cudaFree(b->out);
@@ -1671,6 +1674,37 @@ int lbm_gpu_box_test_wait(lbm_gpu_ctx* ctx, int64_t limit_ns, int32_t starve) {
   drop_graphs(b);  // the graphs hold the old launch parameters
   b->wait_limit_ns = static_cast<uint64_t>(limit_ns);
   b->wait_starve   = starve;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_set_slice_omega(lbm_gpu_ctx* ctx, const double* omega, int32_t n) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b) return LBM_ERR_INVALID;
+  if(b->desc.equation != LBM_NAVIER_STOKES) return LBM_ERR_UNSUPPORTED;
+  cudaStream_t s = lbm_internal_stream(ctx);
+  if(cudaStreamSynchronize(s) != cudaSuccess) return LBM_ERR_CUDA;
+  if(!omega) {
+    drop_graphs(b);  // the graphs hold the old launch parameters
+    b->p.slice_omega   = nullptr;
+    b->p.slice_omega_f = nullptr;
+    return LBM_OK;
+  }
+  if(n != b->p.nz) return LBM_ERR_INVALID;
+  std::vector<float> of(n);
+  for(int z = 0; z < n; ++z) {
+    if(!(omega[z] > 0.0 && omega[z] < 2.0)) return LBM_ERR_INVALID;
+    of[z] = static_cast<float>(omega[z]);
+  }
+  if(!b->slice_omega) {
+    if(cudaMalloc(&b->slice_omega, sizeof(double) * n) != cudaSuccess) return LBM_ERR_NOMEM;
+    if(cudaMalloc(&b->slice_omega_f, sizeof(float) * n) != cudaSuccess) return LBM_ERR_NOMEM;
+  }
+  if(cudaMemcpy(b->slice_omega, omega, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+     cudaMemcpy(b->slice_omega_f, of.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return LBM_ERR_CUDA;
+  drop_graphs(b);
+  b->p.slice_omega   = b->slice_omega;
+  b->p.slice_omega_f = b->slice_omega_f;
   return LBM_OK;
 }
 

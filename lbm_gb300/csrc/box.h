@@ -44,6 +44,9 @@ struct BoxParams {
   // stream); shift_u_d: the same U in double precision
   float   shift_u;
   double  shift_u_d;
+  // per-z-slice relaxation rates (nz values each) or nullptr: one rate
+  const double* slice_omega;
+  const float*  slice_omega_f;
   const uint8_t* flags;     // ncells
   const double*  dirichlet; // ncells Poisson Dirichlet values or nullptr
   void*   pop;              // Q planes of nalloc values of the storage type
@@ -64,6 +67,8 @@ struct BoxState {
   void*        pop_alloc = nullptr;  // the allocation: one guard plane, Q planes, the outlet ghost plane
   uint8_t*     flags = nullptr;
   double*      dirichlet = nullptr;
+  double*      slice_omega   = nullptr;  // per-z-slice relaxation rates (lbm_gpu_box_set_slice_omega)
+  float*       slice_omega_f = nullptr;
   void*        mom   = nullptr;
   double*      partials = nullptr;     // residual partials (one per step block and variable)
   double*      partials_mm = nullptr;  // mass / momentum partials

@@ -155,22 +155,25 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
   return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
 }
 
-// The collision of one cell.  FP64 arithmetic (FP64 storage) works on the
-// scaled deviation v; FP32 arithmetic (the other storages) on the state
-// shifted to the free stream (collide_ns_shifted, U = P.shift_u).
+// The collision of one cell of z-slice z.  FP64 arithmetic (FP64 storage)
+// works on the scaled deviation v; FP32 arithmetic (the other storages) on
+// the state shifted to the free stream (collide_ns_shifted, U = P.shift_u).
+// The relaxation rate is the slice's where the box has one per slice.
 template <int LAT, int EQ, class C>
-__device__ __forceinline__ void collide(const BoxParams& P, C* v, C* mom_out) {
+__device__ __forceinline__ void collide(const BoxParams& P, int z, C* v, C* mom_out) {
   if constexpr(EQ == LBM_NAVIER_STOKES) {
     C F[3];
     F[0] = prm<C>(P.force[0], P.force_f[0]);
     F[1] = prm<C>(P.force[1], P.force_f[1]);
     F[2] = prm<C>(P.force[2], P.force_f[2]);
     if constexpr(sizeof(C) == 4) {
-      if(P.has_force) collide_ns_shifted<LAT, true>(P.omega_f, true, F, P.shift_u, v, mom_out);
-      else collide_ns_shifted<LAT, false>(P.omega_f, false, F, P.shift_u, v, mom_out);
+      const float om = P.slice_omega_f ? P.slice_omega_f[z] : P.omega_f;
+      if(P.has_force) collide_ns_shifted<LAT, true>(om, true, F, P.shift_u, v, mom_out);
+      else collide_ns_shifted<LAT, false>(om, false, F, P.shift_u, v, mom_out);
     } else {
-      if(P.has_force) collide_ns<LAT, C, true>(prm<C>(P.omega, P.omega_f), true, F, v, mom_out);
-      else collide_ns<LAT, C, false>(prm<C>(P.omega, P.omega_f), false, F, v, mom_out);
+      const C om = P.slice_omega ? static_cast<C>(P.slice_omega[z]) : prm<C>(P.omega, P.omega_f);
+      if(P.has_force) collide_ns<LAT, C, true>(om, true, F, v, mom_out);
+      else collide_ns<LAT, C, false>(om, false, F, v, mom_out);
     }
   } else {
     collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,

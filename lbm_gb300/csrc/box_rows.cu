@@ -133,7 +133,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
       if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
       else f[q] = S::load(bx[q * WR]);
     });
-    collide<LAT, EQ, C>(P, f, nullptr);
+    collide<LAT, EQ, C>(P, z, f, nullptr);
   } else {
     const bool emit = ODD ? (special && type == LBM_CELL_INLET) : (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     if(emit) {
@@ -166,7 +166,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
           });
         }
       }
-      collide<LAT, EQ, C>(P, f, nullptr);
+      collide<LAT, EQ, C>(P, z, f, nullptr);
     }
     __syncwarp(active);  // every lane's staged reads come before any lane's stores
   }

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kSeg + 32, min_ctas<ST, MOM>()) k_box_tma(BoxP
             });
           }
         }
-        collide<LAT, EQ, C>(P, f, MOM ? mom : nullptr);
+        collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
       }
       moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
       if constexpr(!ODD) {

@@ -14,7 +14,7 @@ import ctypes as C
 import math
 import os
 import sys
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -285,6 +285,16 @@ class BoxSolver:
         ms = C.c_double()
         check(self._lib.lbm_gpu_box_time_steps(self.ctx, int(n), C.byref(ms)), self.ctx, "time_steps")
         return ms.value
+
+    def set_slice_omega(self, omegas: Optional[Sequence[float]]):
+        """One relaxation rate per z-slice (Navier-Stokes boxes): the slices of
+        a 2D box become a sweep over Reynolds number in one launch per step;
+        None restores the box's single rate."""
+        if omegas is None:
+            check(self._lib.lbm_gpu_box_set_slice_omega(self.ctx, None, 0), self.ctx, "box_set_slice_omega")
+            return
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        check(self._lib.lbm_gpu_box_set_slice_omega(self.ctx, _ptr(om), int(om.size)), self.ctx, "box_set_slice_omega")
 
     def threads_per_block(self) -> int:
         t = C.c_int32()

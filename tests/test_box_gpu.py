@@ -179,7 +179,9 @@ def test_set_populations_from_page_locked_memory(case, storage):
     assert np.array_equal(a.populations(), b.populations())
 
 
-@pytest.mark.parametrize("storage,bound", [("f32", 1e-5), ("f16dev", 5e-3), ("bf16dev", 5e-2)])
+# twice the errors measured on a GB300 (8.0e-7, 2.04e-4, 1.21e-3): a start
+# from rest into an inlet flow, the transient in which rounding costs most
+@pytest.mark.parametrize("storage,bound", [("f32", 1.6e-6), ("f16dev", 4.1e-4), ("bf16dev", 2.4e-3)])
 def test_reduced_precision_storage_against_fp64(storage, bound):
     ref, _ = make_pair("d3q19_sphere_open", "f64")
     low, _ = make_pair("d3q19_sphere_open", storage)
@@ -224,6 +226,47 @@ def test_reduced_precision_storage_long_horizon(storage):
     assert err <= 2.0 * LONG_HORIZON_MEASURED[storage]
     for sv in sol.values():
         sv.close()
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16dev"])
+def test_slices_with_their_own_rates_step_as_separate_boxes(storage):
+    """A sweep: three inlet-driven cylinder channels of different Reynolds
+    numbers (relaxation rates) as the z-slices of one D2Q9 box, each slice at
+    its own rate (lbm_gpu_box_set_slice_omega), step bit for bit as three boxes
+    of their own."""
+    from lbm_gb300 import cases
+
+    chans = [cases.cylinder_channel(s, nx=96, ny=32) for s in (3, 5, 8)]
+    assert len({c["tau"] for c in chans}) == 3
+    st = cases.stacked_sweep(chans)
+    g = BoxSolver(st["lattice"], st["shape"], st["omega"], storage, **cases.box_kwargs(st))
+    g.set_slice_omega(st["slice_omega"])
+    g.initial_condition()
+    g.step(61)
+    f = g.populations()
+    nxy = 96 * 32
+    for k, c in enumerate(chans):
+        one = cases.stacked_sweep([c])
+        s1 = BoxSolver(one["lattice"], one["shape"], 1.0 / c["tau"], storage, **cases.box_kwargs(one))
+        s1.initial_condition()
+        s1.step(61)
+        assert np.array_equal(f[:, k * nxy:(k + 1) * nxy], s1.populations()), k
+        s1.close()
+    # back to the box's single rate: every slice at the first channel's
+    g.set_slice_omega(None)
+    g.initial_condition()
+    g.step(8)
+    one = cases.stacked_sweep([chans[1]])
+    s1 = BoxSolver(one["lattice"], one["shape"], 1.0 / chans[0]["tau"], storage, **cases.box_kwargs(one))
+    s1.initial_condition()
+    s1.step(8)
+    assert np.array_equal(g.populations()[:, nxy:2 * nxy], s1.populations())
+    with pytest.raises(LBMError):
+        g.set_slice_omega([1.2, 1.3])  # not one rate per slice
+    with pytest.raises(LBMError):
+        g.set_slice_omega([1.2, 2.5, 1.3])  # outside (0, 2)
+    g.close()
+    s1.close()
 
 
 def test_mass_conservation_closed_box():
