@@ -784,7 +784,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
     // the row-staged kernel takes its outlet face cells' upstream values from
     // its own staged rows (when the outlet and upstream cells share a warp)
     const int  k    = odd ? b->kind_odd : b->kind_even;
-    const bool skip = k == LBM_BOX_KERNEL_ROWS && mom == 0 && box_rows_outlet_inline(b);
+    const bool skip = k == LBM_BOX_KERNEL_ROWS && box_rows_outlet_inline(b);
     if(odd) k_box_outlet<LAT, ST, true><<<go, 128, 0, s>>>(b->p, skip);
     else k_box_outlet<LAT, ST, false><<<go, 128, 0, s>>>(b->p, skip);
   }
@@ -793,7 +793,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   const int      kind   = odd ? b->kind_odd : b->kind_even;
   const bool     staged = kind == LBM_BOX_KERNEL_STAGED;
   const bool     paired = kind == LBM_BOX_KERNEL_PAIRED && mom == 0;  // residual steps use the per-thread kernel
-  const bool     rows   = kind == LBM_BOX_KERNEL_ROWS && mom == 0;    // like the per-thread kernel: XFACE cells in line
+  const bool     rows   = kind == LBM_BOX_KERNEL_ROWS;                // like the per-thread kernel: XFACE cells in line
   // the per-thread odd kernel steps the XFACE cells itself; with the others the
   // boundary kernel takes them too (they close its list)
   // and its SFACE cells are taken by the boundary kernel's face blocks
@@ -813,7 +813,7 @@ cudaError_t launch_step(BoxState* b, bool odd, int mom, cudaStream_t s, cudaEven
   }
   if(rows) {
     // before the boundary kernel, whose cells' slots it writes back unchanged
-    const cudaError_t e = box_rows_bulk(b, odd, s);
+    const cudaError_t e = box_rows_bulk(b, odd, mom, s, &nbulk);
     if(e != cudaSuccess) return e;
   }
   if(odd) {

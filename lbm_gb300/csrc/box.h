@@ -112,14 +112,16 @@ void        box_destroy(BoxState* b);
 // the launch; *slots = residual partial slots the launch writes
 bool        box_tma_supported(const BoxState* b);
 cudaError_t box_tma_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* slots);
-// row-staged bulk kernel (box_rows.cu), plain steps only: whether the box
-// qualifies, and the launch.  Its odd step must run before the boundary
-// kernel: it writes back the unchanged slots of the cells it does not step.
+// row-staged bulk kernel (box_rows.cu): whether the box qualifies, and the
+// launch (mom: 0 plain step, 1 / 2 the two halves of a residual step; *nbulk
+// gets the residual slots it writes).  Its odd step must run before the
+// boundary kernel: it writes back the unchanged slots of the cells it does
+// not step.
 bool        box_rows_supported(const BoxState* b);
 // whether the row-staged kernel reads its XFACE outlet cells' upstream
 // values from its staged rows (then the ghost fill skips those cells)
 bool        box_rows_outlet_inline(const BoxState* b);
-cudaError_t box_rows_bulk(BoxState* b, bool odd, cudaStream_t s);
+cudaError_t box_rows_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* nbulk);
 
 }  // namespace lbm
 

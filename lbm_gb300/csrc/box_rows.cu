@@ -101,9 +101,11 @@ struct RowList {
 };
 
 // One cell of a staged row.  bx: the cell's element in plane 0 of the stage
-// (index H + x).
-template <int LAT, int EQ, int ST, bool ODD, int WR>
-__device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z, bool outlet_inline) {
+// (index H + x).  MOM: 0 plain step, 1 also write the cell's moments, 2 also
+// add |moments - previous moments| to dacc (the cell's residual share).
+template <int LAT, int EQ, int ST, bool ODD, int WR, int MOM, int NV>
+__device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z, bool outlet_inline,
+                                         typename Store<ST>::C* dacc) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -122,6 +124,10 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
     special = type != LBM_CELL_FLUID;
   }
   if(!work) return;
+  C prev[NV], mom[NV];
+  prefetch_moments<C, MOM, NV>(P, cell, prev);
+#pragma unroll
+  for(int k = 0; k < NV; ++k) mom[k] = 0;
   // one vote per warp: warps of plain fluid cells take the path without the
   // inlet / outlet / Dirichlet branches
   const unsigned active      = __activemask();
@@ -133,7 +139,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
       if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
       else f[q] = S::load(bx[q * WR]);
     });
-    collide<LAT, EQ, C>(P, z, f, nullptr);
+    collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
   } else {
     const bool emit = ODD ? (special && type == LBM_CELL_INLET) : (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     if(emit) {
@@ -166,9 +172,17 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
           });
         }
       }
-      collide<LAT, EQ, C>(P, z, f, nullptr);
+      collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
     }
     __syncwarp(active);  // every lane's staged reads come before any lane's stores
+  }
+  if constexpr(MOM != 0) {
+    C diff[NV];
+    moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
+    if constexpr(MOM == 2) {
+#pragma unroll
+      for(int k = 0; k < NV; ++k) dacc[k] += diff[k];
+    }
   }
   static_for<Q>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
@@ -184,12 +198,14 @@ constexpr int row_min_ctas() {
   return ST == LBM_STORE_F64 ? 1 : (ST == LBM_STORE_F32 ? 2 : LBM_ROWS_CTAS_16);
 }
 
-template <int LAT, int EQ, int ST, bool ODD, int K>
+template <int LAT, int EQ, int ST, bool ODD, int K, int MOM>
 __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxParams P, RowList R) {
   using L             = Lattice<LAT>;
   using S             = Store<ST>;
   using T             = typename S::T;
+  using C             = typename S::C;
   constexpr int Q     = L::Q;
+  constexpr int NV    = EQ == LBM_NAVIER_STOKES ? L::D + 1 : 1;
   constexpr int H     = row_halo<T>();
   constexpr int NST   = row_stages<T>();
   constexpr int WR    = row_width<T, K>();
@@ -295,22 +311,29 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
       return;
     }
     T* const stage = buf + st * STAGE + H;
+    C        dacc[NV];
+#pragma unroll
+    for(int k = 0; k < NV; ++k) dacc[k] = C(0);
 #pragma unroll 1
-    for(int x = tid; x < nx; x += kRowThreads) row_cell<LAT, EQ, ST, ODD, WR>(P, stage + x, x, y, z, R.outlet_inline != 0);
+    for(int x = tid; x < nx; x += kRowThreads)
+      row_cell<LAT, EQ, ST, ODD, WR, MOM, NV>(P, stage + x, x, y, z, R.outlet_inline != 0, dacc);
     fence_async_smem();  // this thread's writes are visible to the bulk stores
     __syncwarp();
     if(lane == 0) mbar_arrive(smem_u32(&done[st]));
+    // residual share of the row: one slot per (row, cell warp)
+    if constexpr(MOM == 2)
+      warp_partials<NV>(dacc, P.partials, P.partial_stride, static_cast<int64_t>(first + i) * kRowWarps + (warp - 1));
   }
 }
 
-template <int LAT, int EQ, int ST, bool ODD, int K>
+template <int LAT, int EQ, int ST, bool ODD, int K, int MOM>
 cudaError_t launch_rows_one(BoxState* b, const RowList& R, cudaStream_t s) {
   using T           = typename Store<ST>::T;
   constexpr size_t smem = row_smem<LAT, T, K>();
   if constexpr(smem > kRowSmemMax) {
     return cudaErrorInvalidValue;
   } else {
-    auto kern = k_box_rows<LAT, EQ, ST, ODD, K>;
+    auto kern = k_box_rows<LAT, EQ, ST, ODD, K, MOM>;
     // resident CTAs on the whole GPU, worked out once per instantiation
     static int resident = 0;
     if(resident == 0) {
@@ -338,8 +361,21 @@ int row_k(int nx) {
   return 0;
 }
 
+template <int LAT, int EQ, int ST, int K>
+cudaError_t launch_rows_k(BoxState* b, bool odd, int mom, const RowList& R, cudaStream_t s) {
+  if(odd) {
+    if(mom == 0) return launch_rows_one<LAT, EQ, ST, true, K, 0>(b, R, s);
+    if(mom == 1) return launch_rows_one<LAT, EQ, ST, true, K, 1>(b, R, s);
+    return launch_rows_one<LAT, EQ, ST, true, K, 2>(b, R, s);
+  }
+  if(mom == 0) return launch_rows_one<LAT, EQ, ST, false, K, 0>(b, R, s);
+  if(mom == 1) return launch_rows_one<LAT, EQ, ST, false, K, 1>(b, R, s);
+  return launch_rows_one<LAT, EQ, ST, false, K, 2>(b, R, s);
+}
+
+// *nbulk: the residual slots the launch writes (one per row and cell warp)
 template <int LAT, int EQ, int ST>
-cudaError_t launch_rows(BoxState* b, bool odd, cudaStream_t s) {
+cudaError_t launch_rows(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* nbulk) {
   using L = Lattice<LAT>;
   using T = typename Store<ST>::T;
   RowList R{};
@@ -361,10 +397,11 @@ cudaError_t launch_rows(BoxState* b, bool odd, cudaStream_t s) {
   R.limit_ns = b->wait_limit_ns;
   R.starve   = b->wait_starve;
   R.outlet_inline = box_rows_outlet_inline(b) ? 1 : 0;
+  if(nbulk) *nbulk = static_cast<int64_t>(R.count) * kRowWarps;
   if(R.count == 0) return cudaSuccess;
   const int k = row_k(b->p.nx);
-  if(k == 2) return odd ? launch_rows_one<LAT, EQ, ST, true, 2>(b, R, s) : launch_rows_one<LAT, EQ, ST, false, 2>(b, R, s);
-  if(k == 4) return odd ? launch_rows_one<LAT, EQ, ST, true, 4>(b, R, s) : launch_rows_one<LAT, EQ, ST, false, 4>(b, R, s);
+  if(k == 2) return launch_rows_k<LAT, EQ, ST, 2>(b, odd, mom, R, s);
+  if(k == 4) return launch_rows_k<LAT, EQ, ST, 4>(b, odd, mom, R, s);
   return cudaErrorInvalidValue;
 }
 
@@ -410,19 +447,19 @@ bool box_rows_supported(const BoxState* b) {
   return smem > 0 && smem <= kRowSmemMax;
 }
 
-cudaError_t box_rows_bulk(BoxState* b, bool odd, cudaStream_t s) {
+cudaError_t box_rows_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_t* nbulk) {
   const int key = b->desc.lattice * 100 + b->desc.equation * 10 + b->desc.storage;
   switch(key) {
-    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F64>(b, odd, s);
-    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F32>(b, odd, s);
-    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(b, odd, s);
-    case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(b, odd, s);
-    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F64>(b, odd, s);
-    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F32>(b, odd, s);
-    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(b, odd, s);
-    case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(b, odd, s);
-    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F64>(b, odd, s);
-    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F32>(b, odd, s);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F64>(b, odd, mom, s, nbulk);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F32>(b, odd, mom, s, nbulk);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F64>(b, odd, mom, s, nbulk);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F32>(b, odd, mom, s, nbulk);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F64>(b, odd, mom, s, nbulk);
+    case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F32>(b, odd, mom, s, nbulk);
     default: return cudaErrorInvalidValue;
   }
 }
