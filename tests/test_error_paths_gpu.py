@@ -74,7 +74,7 @@ def test_staged_kernel_wait_timeout_reports_timeout(storage, kernel):
     assert lib.lbm_gpu_box_test_wait(g.ctx, 1_000_000, 1) == 0  # 1 ms per wait, first segments never armed
     g.initial_condition()
     with pytest.raises(LBMError) as e:
-        g.step(4)  # two plain steps (the row-staged kernel runs plain steps only), then two residual steps
+        g.step(4)  # two plain steps, then the two halves of a residual step
     assert e.value.code == TIMEOUT
     # out-of-range settings are rejected
     assert lib.lbm_gpu_box_test_wait(g.ctx, 0, 0) == -1
