@@ -48,6 +48,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "box.h"
 #include "box_device.cuh"
@@ -84,11 +85,22 @@ template <class T, int K>
 constexpr int row_width() {
   return 256 * K + 2 * row_halo<T>();
 }
-template <int LAT, class T, int K>
-constexpr size_t row_smem() {
-  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 2 * row_stages<T>();
+// residual steps (MOM = 2): the previous moments of a cell thread's cells in
+// the row (at most K, NV each, in the arithmetic type), fetched into shared
+// memory with cp.async when the row starts and read after the collision, so
+// that they hold no registers across it
+template <class T, int K, int MOM>
+constexpr size_t row_prev_bytes() {
+  using C = typename std::conditional<sizeof(T) == 8, double, float>::type;
+  return MOM == 2 ? sizeof(C) * static_cast<size_t>(K) * 4 * kRowThreads : 0;
 }
-constexpr size_t kRowSmemMax = 200 * 1024;
+template <int LAT, class T, int K, int MOM = 0>
+constexpr size_t row_smem() {
+  return sizeof(T) * row_stages<T>() * Lattice<LAT>::Q * row_width<T, K>() + sizeof(uint64_t) * 2 * row_stages<T>() +
+         row_prev_bytes<T, K, MOM>();
+}
+constexpr size_t kRowSmemMax = 200 * 1024;  // the plain step's stages (box_rows_supported)
+constexpr size_t kRowSmemHw  = 227 * 1024;  // per-CTA limit: the residual step's prefetch area comes on top
 
 struct RowList {
   FastDiv  nrows;     // rows per z-slab in the list
@@ -100,12 +112,21 @@ struct RowList {
   int      outlet_inline;  // XFACE outlet cells read their upstream cell's values from the staged row
 };
 
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// one element global -> shared without registers (cp.async, 4 or 8 bytes)
+template <class C>
+__device__ __forceinline__ void cp_async_elem(C* dst, const C* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"(static_cast<int>(sizeof(C))) : "memory");
+}
+
 // One cell of a staged row.  bx: the cell's element in plane 0 of the stage
 // (index H + x).  MOM: 0 plain step, 1 also write the cell's moments, 2 also
-// add |moments - previous moments| to dacc (the cell's residual share).
+// add |moments - previous moments| to dacc (the cell's residual share); the
+// previous moments are at prev_s[v * kRowThreads], fetched with cp.async.
 template <int LAT, int EQ, int ST, bool ODD, int WR, int MOM, int NV>
 __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z, bool outlet_inline,
-                                         typename Store<ST>::C* dacc) {
+                                         typename Store<ST>::C* dacc, const typename Store<ST>::C* prev_s) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -124,8 +145,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
     special = type != LBM_CELL_FLUID;
   }
   if(!work) return;
-  C prev[NV], mom[NV];
-  prefetch_moments<C, MOM, NV>(P, cell, prev);
+  C mom[NV];
 #pragma unroll
   for(int k = 0; k < NV; ++k) mom[k] = 0;
   // one vote per warp: warps of plain fluid cells take the path without the
@@ -177,7 +197,12 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
     __syncwarp(active);  // every lane's staged reads come before any lane's stores
   }
   if constexpr(MOM != 0) {
-    C diff[NV];
+    C prev[NV], diff[NV];
+    if constexpr(MOM == 2) {
+      cp_async_wait_all();
+#pragma unroll
+      for(int k = 0; k < NV; ++k) prev[k] = prev_s[k * kRowThreads];
+    }
     moments_io<LAT, EQ, C, MOM, NV>(P, cell, mom, prev, diff);
     if constexpr(MOM == 2) {
 #pragma unroll
@@ -214,6 +239,7 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
   T*        buf  = reinterpret_cast<T*>(smem);
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + sizeof(T) * NST * STAGE);  // the row's loads landed
   uint64_t* done = full + NST;                                                   // the cell warps wrote the row
+  C*        prevbuf = reinterpret_cast<C*>(done + NST);                          // MOM = 2: previous moments (4 per cell)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G    = static_cast<int>(gridDim.x);
@@ -314,9 +340,25 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
     C        dacc[NV];
 #pragma unroll
     for(int k = 0; k < NV; ++k) dacc[k] = C(0);
+    if constexpr(MOM == 2) {
+      // the previous moments of this thread's cells in the row, in flight
+      // while the cells collide
+      const C*      M   = static_cast<const C*>(P.mom);
+      const int64_t row = static_cast<int64_t>(nx) * (y + static_cast<int64_t>(ny) * z);
+      int           j   = 0;
 #pragma unroll 1
-    for(int x = tid; x < nx; x += kRowThreads)
-      row_cell<LAT, EQ, ST, ODD, WR, MOM, NV>(P, stage + x, x, y, z, R.outlet_inline != 0, dacc);
+      for(int x = tid; x < nx; x += kRowThreads, ++j)
+#pragma unroll
+        for(int v = 0; v < NV; ++v) cp_async_elem(prevbuf + (j * 4 + v) * kRowThreads + tid, M + v * P.ncells + row + x);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    {
+      int j = 0;
+#pragma unroll 1
+      for(int x = tid; x < nx; x += kRowThreads, ++j)
+        row_cell<LAT, EQ, ST, ODD, WR, MOM, NV>(P, stage + x, x, y, z, R.outlet_inline != 0, dacc, prevbuf + j * 4 * kRowThreads + tid);
+    }
+    if constexpr(MOM == 2) cp_async_wait_all();  // none left in flight (cells that did no work never waited)
     fence_async_smem();  // this thread's writes are visible to the bulk stores
     __syncwarp();
     if(lane == 0) mbar_arrive(smem_u32(&done[st]));
@@ -329,8 +371,8 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
 template <int LAT, int EQ, int ST, bool ODD, int K, int MOM>
 cudaError_t launch_rows_one(BoxState* b, const RowList& R, cudaStream_t s) {
   using T           = typename Store<ST>::T;
-  constexpr size_t smem = row_smem<LAT, T, K>();
-  if constexpr(smem > kRowSmemMax) {
+  constexpr size_t smem = row_smem<LAT, T, K, MOM>();
+  if constexpr(smem > (MOM == 2 ? kRowSmemHw : kRowSmemMax)) {
     return cudaErrorInvalidValue;
   } else {
     auto kern = k_box_rows<LAT, EQ, ST, ODD, K, MOM>;

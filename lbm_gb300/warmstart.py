@@ -532,28 +532,25 @@ def predict_fields(net: "UNet", chans: List[Dict], scales: Scales,
     return out
 
 
-def flux_balance(chans: List[Dict], fields, iters: int = 2, settle: int = 64, window: Optional[int] = None):
+def flux_balance(chans: List[Dict], fields, iters: int = 3, settle: int = 0, window: int = 2):
     """Rescale each predicted field so that the drag of the walls and
     cylinders balances the body force, as it does in the steady state.
 
-    The slowest mode of a forced periodic channel is its flow rate, which
-    relaxes on the viscous time ny^2 / nu; a network with a finite receptive
-    field predicts the local flow pattern far better than the channel-wide
-    flow rate (set by every obstacle along the channel).  For each channel the
-    predicted state steps in FP64: after `settle` steps (the fast
-    non-equilibrium transient of the initialisation), the change of its total
-    x momentum over `window` steps, per step, is the body force minus the
-    drag, D = F N - dP/dt (the window, by default one crossing of the
-    periodic length at the speed of sound, averages the pressure waves out).
-    Velocity and density deviation are scaled by F N / D, as a Stokes flow
-    scales with its forcing; `iters` fixed-point passes take up the inertial
-    part.  Returns the corrected fields and each channel's total scale."""
+    The network predicts the flow pattern per unit flow rate
+    (normalize_by_flux); the flow rate of a channel is set by every obstacle
+    along it.  For each channel the predicted state steps in FP64, and the
+    change of its total x momentum per step over `window` steps (after
+    `settle`) is the body force minus the drag, D = F N - dP/dt.  Velocity and
+    density deviation are scaled by F N / D, as a Stokes flow scales with its
+    forcing; `iters` fixed-point passes take up the inertial part.  The
+    estimate is taken over the first steps: the flow rate relaxes towards the
+    balance on the time P / F (a few hundred steps), so a longer window
+    measures a drag already partly relaxed.  Returns the corrected fields and
+    each channel's total scale."""
     from .solver import BoxSolver
 
     st = cases.stacked_forced(chans)
     n = len(chans)
-    if window is None:
-        window = int(math.ceil(math.sqrt(3.0) * chans[0]["shape"][0]))
     fluid = np.stack([c["flags"] != cases.SOLID for c in chans]).reshape(n, -1)
     force = np.array([c["g"] for c in chans]) * fluid.sum(axis=1)
     fields = [(r.copy(), ux.copy(), uy.copy()) for r, ux, uy in fields]
@@ -562,7 +559,8 @@ def flux_balance(chans: List[Dict], fields, iters: int = 2, settle: int = 64, wi
     try:
         for _ in range(iters):
             g.set_populations(warm_start_populations(chans, fields))
-            g.step(settle)
+            if settle:
+                g.step(settle)
             r0, u0 = g.moments()
             g.step(window)
             r1, u1 = g.moments()
