@@ -406,14 +406,73 @@ def period2_filter(g) -> None:
     g.set_populations(0.5 * (s0 + s1))
 
 
+def channel_momentum(g, n: int) -> np.ndarray:
+    """Total x momentum of each of the n stacked channels."""
+    rho, u = g.moments()
+    return (rho * u[0]).reshape(n, -1).sum(axis=1)
+
+
+def aitken_scales(pa: np.ndarray, pb: np.ndarray, pc: np.ndarray) -> np.ndarray:
+    """Per channel, P_inf / P(c) for momenta sampled at equally spaced steps
+    a < b < c of an exponential relaxation P(t) = P_inf + A exp(-t / T):
+    with r = (P(c) - P(b)) / (P(b) - P(a)) = exp(-(c - b) / T), Aitken's
+    extrapolation P_inf = P(c) + (P(c) - P(b)) r / (1 - r).  1 where the samples
+    do not contract (0 < r < 0.95), clipped to [0.2, 5]."""
+    pa, pb, pc = (np.asarray(v, dtype=np.float64) for v in (pa, pb, pc))
+    d1, d2 = pb - pa, pc - pb
+    r = np.divide(d2, d1, out=np.zeros_like(d2), where=np.abs(d1) > 0)
+    ok = (r > 0.0) & (r < 0.95) & (np.abs(pc) > 0)
+    p_inf = pc + d2 * r / np.where(ok, 1.0 - r, 1.0)
+    return np.where(ok, np.clip(p_inf / np.where(ok, pc, 1.0), 0.2, 5.0), 1.0)
+
+
+def rescale_flow(g, chans: List[Dict], scale: np.ndarray) -> None:
+    """Scale the flow of each stacked channel k by scale[k], as a Stokes flow
+    scales with its forcing: f -> f_eq(1 + s (rho - 1), s u) + s (f - f_eq(rho, u))
+    in every fluid cell (u the Guo velocity (j + F / 2) / rho)."""
+    f = g.populations()
+    n = len(chans)
+    ny_nx = f.shape[1] // n
+    rho = f.sum(axis=0)
+    jx = (C_D2Q9[:, 0, None] * f).sum(axis=0)
+    jy = (C_D2Q9[:, 1, None] * f).sum(axis=0)
+    fluid = np.concatenate([(c["flags"] != cases.SOLID).reshape(-1) for c in chans])
+    gx = np.concatenate([np.full(ny_nx, c["g"]) for c in chans])
+    sc = np.repeat(np.asarray(scale, dtype=np.float64), ny_nx)
+    rho = np.where(fluid, rho, 1.0)  # solids keep their populations below; no division by their (zero) density
+    ux = np.where(fluid, (jx + 0.5 * gx) / rho, 0.0)
+    uy = np.where(fluid, jy / rho, 0.0)
+
+    def feq(r, vx, vy):
+        usq = vx * vx + vy * vy
+        out = np.empty((9,) + r.shape)
+        for i in range(9):
+            cu = C_D2Q9[i, 0] * vx + C_D2Q9[i, 1] * vy
+            out[i] = W_D2Q9[i] * r * (1 + 3 * cu + 4.5 * cu * cu - 1.5 * usq)
+        return out
+
+    new = feq(1.0 + sc * (rho - 1.0), sc * ux, sc * uy) + sc * (f - feq(rho, ux, uy))
+    g.set_populations(np.where(fluid[None, :], new, f))
+
+
 def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[float] = None, check: int = 2000,
-              init: Optional[np.ndarray] = None, filters=(0, 2000)) -> Dict:
+              init: Optional[np.ndarray] = None, filters=(0, 2000), project: Optional[Tuple[int, int, int]] = None) -> Dict:
     """Forced channels sharing one Re as the z-slices of one D2Q9 box, from
     rest (or from populations `init`, (9, ncells)), for max_steps or until the
     residual summed over the slices, divided by their number, is below tol
     (checked every `check` steps: the reference's convergence test with
     conv_interval = check).  A warm start applies period2_filter at the steps
-    in `filters`.  Returns fields, steps, wall time, residual."""
+    in `filters` (a start from rest too, when `init` holds the rest state).
+
+    project = (a, b, c): the flow-rate projection.  The slowest mode of a
+    forced channel is its flow rate, which relaxes exponentially towards the
+    balance of drag and body force on the time P / F (thousands of steps for
+    the 128-high channels).  The total x momentum of each channel is sampled
+    at steps a < b < c (b - a = c - b); Aitken's extrapolation of the three
+    gives the momentum P_inf the channel relaxes to, and at step c the flow
+    is scaled by P_inf / P(c) (rescale_flow), which removes that mode.  A
+    channel whose samples are not a contracting monotone sequence is left as
+    it is.  Returns fields, steps, wall time, residual and the scales."""
     from .solver import BoxSolver
 
     st = cases.stacked_forced(chans)
@@ -422,6 +481,9 @@ def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[flo
     g.synchronize()
     t0 = time.perf_counter()
     pending = sorted(filters) if init is not None else []
+    samples = list(project) if project else []
+    moms: List[np.ndarray] = []
+    scales = None
     if init is not None:
         g.set_populations(init)
     n = len(chans)
@@ -432,24 +494,33 @@ def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[flo
             period2_filter(g)
             done += 1
             continue
+        if samples and samples[0] <= done:
+            samples.pop(0)
+            moms.append(channel_momentum(g, n))
+            if len(moms) == 3:
+                scales = aitken_scales(*moms)
+                rescale_flow(g, chans, scales)
+            continue
         k = min(check, max_steps - done)
         if pending:
             k = min(k, max(2, pending[0] - done))
+        if samples:
+            k = min(k, samples[0] - done)
         g.step(k)
         done += k
-        if tol is not None:
+        if tol is not None and k >= 2:
             res = g.residual() / n
             if float(np.max(res)) < tol:
                 break
     g.synchronize()
     wall = time.perf_counter() - t0
-    if tol is None:
+    if tol is None or not np.all(np.isfinite(res)):
         res = g.residual() / n
     rho, u = g.moments()
     nx, ny = chans[0]["shape"]
     g.close()
     return dict(rho=rho.reshape(n, ny, nx), ux=u[0].reshape(n, ny, nx), uy=u[1].reshape(n, ny, nx), steps=done, wall=wall,
-                residual=float(np.max(res)))
+                residual=float(np.max(res)), flow_scales=None if scales is None else [float(x) for x in scales])
 
 
 def make_dataset(seeds: List[int], per_batch: int, steps: int, storage: str = "f32", nx: int = 512, ny: int = 128,
@@ -584,7 +655,7 @@ def warm_start_populations(chans: List[Dict], fields) -> np.ndarray:
 def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 300000, epochs: int = 20, n_eval: int = 16,
                per_eval: int = 8, tol: float = 1e-8, max_steps: int = 1500000, nx: int = 511, ny: int = 128, batch: int = 8,
                re_range=(20.0, 200.0), lr: float = 1e-3, filtered_rest: bool = True, normalize_flux: bool = True,
-               log=print) -> Dict:
+               project: Optional[Tuple[int, int, int]] = (2500, 4500, 6500), log=print) -> Dict:
     """The whole warm-start study: FP32 training fields, training with the
     project's kernels, then for held-out channels the plain FP64 LBM from rest
     and from the network's prediction to the same residual.
@@ -623,10 +694,12 @@ def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 3000
         chans = [cases.forced_channel(100000 + k + j, nx, ny, re=re) for j in range(per_eval)]
         cold = run_stack(chans, "f64", max_steps, tol)
         # the same filters applied from rest, to separate their share of the gain from the network's
-        rest = None
+        rest = rest_p = None
+        rest_init = warm_start_populations(chans, [(np.ones((ny, nx)), np.zeros((ny, nx)), np.zeros((ny, nx))) for _ in chans])
         if filtered_rest:
-            rest = run_stack(chans, "f64", max_steps, tol, init=warm_start_populations(
-                chans, [(np.ones((ny, nx)), np.zeros((ny, nx)), np.zeros((ny, nx))) for _ in chans]))
+            rest = run_stack(chans, "f64", max_steps, tol, init=rest_init)
+            # and with the flow-rate projection, which is physics, not learned
+            rest_p = run_stack(chans, "f64", max_steps, tol, init=rest_init, project=project)
         fluid = np.stack([c["flags"] != cases.SOLID for c in chans])
 
         def err_of(fl):
@@ -644,26 +717,32 @@ def experiment(n_train: int = 1024, per_batch: int = 64, train_steps: int = 3000
         fields_b, alpha = flux_balance(chans, fields)
         init = warm_start_populations(chans, fields_b)
         t_pred_b = time.perf_counter() - tp
-        warm = run_stack(chans, "f64", max_steps, tol, init=init)
+        warm = run_stack(chans, "f64", max_steps, tol, init=init, project=project)
         rows.append(dict(re=re, cold_steps=cold["steps"], cold_wall=cold["wall"], cold_res=cold["residual"],
                          rest_filtered_steps=rest["steps"] if rest else None, rest_filtered_wall=rest["wall"] if rest else None,
+                         rest_projected_steps=rest_p["steps"] if rest_p else None,
+                         rest_projected_wall=rest_p["wall"] if rest_p else None,
+                         rest_projected_scales=rest_p["flow_scales"] if rest_p else None, warm_projected_scales=warm["flow_scales"],
                          net_steps=warm_net["steps"], net_wall=warm_net["wall"] + t_pred, ux_rel_l2_net=err_of(fields),
                          warm_steps=warm["steps"], warm_wall=warm["wall"] + t_pred_b, warm_res=warm["residual"], predict_s=t_pred_b,
                          ux_rel_l2_pred=err_of(fields_b), flux_scale=[float(a) for a in alpha]))
         if log:
             log(f"held-out Re {re:.1f}: cold {cold['steps']} steps {cold['wall']:.1f} s; rest+filters "
-                f"{rest['steps'] if rest else '-'}; net {warm_net['steps']} steps (u_x error {err_of(fields):.3e}); "
-                f"net+flux {warm['steps']} steps {warm['wall'] + t_pred_b:.1f} s (u_x error {err_of(fields_b):.3e})")
+                f"{rest['steps'] if rest else '-'}; rest+filters+projection {rest_p['steps'] if rest_p else '-'}; "
+                f"net {warm_net['steps']} steps (u_x error {err_of(fields):.3e}); "
+                f"warm {warm['steps']} steps {warm['wall'] + t_pred_b:.1f} s (u_x error {err_of(fields_b):.3e})")
     cs = sum(r["cold_steps"] for r in rows)
     ws = sum(r["warm_steps"] for r in rows)
     cw = sum(r["cold_wall"] for r in rows)
     ww = sum(r["warm_wall"] for r in rows)
     nw = sum(r["net_wall"] for r in rows)
     rr = [r for r in rows if r["rest_filtered_wall"] is not None]
+    rcw = sum(r["cold_wall"] for r in rr)
     return dict(n_train=n_train, train_steps=train_steps, epochs=epochs, dataset_s=t_data, train_s=t_train, final_loss=losses[-1],
                 train_tflops=flops / t_train / 1e12, eval=rows, steps_ratio=ws / cs, wall_ratio=ww / cw, net_only_wall_ratio=nw / cw,
-                rest_filtered_wall_ratio=(sum(r["rest_filtered_wall"] for r in rr) / sum(r["cold_wall"] for r in rr)) if rr else None,
-                tol=tol, max_steps=max_steps)
+                rest_filtered_wall_ratio=(sum(r["rest_filtered_wall"] for r in rr) / rcw) if rr else None,
+                rest_projected_wall_ratio=(sum(r["rest_projected_wall"] for r in rr) / rcw) if rr else None,
+                project=list(project) if project else None, tol=tol, max_steps=max_steps)
 
 
 def net_flops(net: "UNet") -> float:
