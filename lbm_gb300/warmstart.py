@@ -472,7 +472,9 @@ def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[flo
     gives the momentum P_inf the channel relaxes to, and at step c the flow
     is scaled by P_inf / P(c) (rescale_flow), which removes that mode.  A
     channel whose samples are not a contracting monotone sequence is left as
-    it is.  Returns fields, steps, wall time, residual and the scales."""
+    it is; the period-2 filter follows the rescaling (the rescaled state has a
+    component along that undamped mode again).  Returns fields, steps, wall
+    time, residual and the scales."""
     from .solver import BoxSolver
 
     st = cases.stacked_forced(chans)
@@ -500,6 +502,10 @@ def run_stack(chans: List[Dict], storage: str, max_steps: int, tol: Optional[flo
             if len(moms) == 3:
                 scales = aitken_scales(*moms)
                 rescale_flow(g, chans, scales)
+                # the rescaled state has a component along the undamped
+                # period-2 mode again: filter it out
+                period2_filter(g)
+                done += 1
             continue
         k = min(check, max_steps - done)
         if pending:
