@@ -19,7 +19,9 @@
  *          6 a 16-bit float of 1 sign, 4 exponent and 11 mantissa bits
  *            (Lehmann et al., Phys. Rev. E 106, 015308 (2022)) of s / S x 4:
  *            12 significant bits, normal range [2^-14, 2), saturating;
- *          8 16-bit fixed point of s: round(s / S x 2^15) / 2^15, saturating
+ *          8 16-bit fixed point of s: round(s / S x 2^15) / 2^15, saturating;
+          9 block floating point of s: per cell, 16-bit integers times one
+            power-of-two scale 2^(e - 15) with 2^e >= the cell's max |s|
  *   arith: 0 FP64 on v; 2 FP32 on the shifted state (the engine's
  *          single-precision collision in the same operation order)
  * out.bin: rho, ux, uy, uz per cell (FP64), x fastest.
@@ -58,6 +60,23 @@ static double round_fp(double x, int p, int emin, double maxv) {
   if(lead < emin) lead = emin;
   const double q = ldexp(1.0, lead - (p - 1));
   return copysign(nearbyint(a / q) * q, x);
+}
+
+/* store 9: the cell's 19 values as 16-bit integers with one power-of-two
+   scale per cell (a shared exponent: block floating point), 2^e >= max |x| */
+static void store_block(double* x) {
+  double m = 0;
+  for(int q = 0; q < 19; ++q) m = fmax(m, fabs(x[q]));
+  if(m == 0) return;
+  int e;
+  frexp(m, &e);
+  const double sc = ldexp(1.0, e - 15);
+  for(int q = 0; q < 19; ++q) {
+    double v = nearbyint(x[q] / sc);
+    if(v > 32767) v = 32767;
+    if(v < -32767) v = -32767;
+    x[q] = v * sc;
+  }
 }
 
 /* the stored value of x (state units: v or s) of direction q, cell i, step t */
@@ -153,8 +172,10 @@ int main(int argc, char** argv) {
   double  feq0[19];
   for(int q = 0; q < 19; ++q) {
     const double cu = C[q][0] * u0;
-    feq0[q]         = store(S * (3 * cu + 4.5 * cu * cu - 1.5 * u0 * u0) - K[q], q, 0, 0);
+    feq0[q]         = S * (3 * cu + 4.5 * cu * cu - 1.5 * u0 * u0) - K[q];
+    if(smode != 9) feq0[q] = store(feq0[q], q, 0, 0);
   }
+  if(smode == 9) store_block(feq0);
   for(int q = 0; q < 19; ++q)
     for(int64_t i = 0; i < N; ++i) f[q * N + i] = fl[i] == 1 ? 0 : feq0[q];
   for(long t = 0; t < steps; ++t) {
@@ -216,7 +237,8 @@ int main(int argc, char** argv) {
           o[q]             = S * (v[q] + om * (veq - v[q])) - K[q];
         }
       }
-      for(int q = 0; q < 19; ++q) fs[q * N + i] = store(o[q], q, (uint32_t)i, (uint32_t)t);
+      if(smode == 9) store_block(o);
+      for(int q = 0; q < 19; ++q) fs[q * N + i] = smode == 9 ? o[q] : store(o[q], q, (uint32_t)i, (uint32_t)t);
     }
 #pragma omp parallel for schedule(static)
     for(int64_t i = 0; i < N; ++i) {

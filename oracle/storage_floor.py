@@ -28,6 +28,7 @@ VARIANTS = [
     (14, 2, "FP16 of the shifted state with stochastic rounding, FP32 arithmetic"),
     (6, 2, "1-4-11 16-bit float of the shifted state, FP32 arithmetic"),
     (8, 2, "16-bit fixed point of the shifted state, FP32 arithmetic"),
+    (9, 2, "16-bit block floating point of the shifted state (one exponent per cell), FP32 arithmetic"),
 ]
 
 
