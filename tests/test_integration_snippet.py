@@ -1,7 +1,7 @@
-"""The C++ binding of the GB300 step in INTEGRATION.md compiles against the
-reference's own LBMSolver (src/lbm/solver.h, src/lbm/solver.cpp).
+"""The C++ binding of the GB300 step in the integration guide compiles
+against the reference's own LBMSolver (src/lbm/solver.h, src/lbm/solver.cpp).
 
-The code block of INTEGRATION.md's C++ section is compiled, with
+The code block of the guide's C++ section is compiled, with
 ``g++ -fsyntax-only``, in a translation unit that includes the reference's
 solver the way the reference harness does (oracle/ref_harness.cpp: the
 reference sources prepared by oracle/build_ref.sh, the serial MPI stub, the
@@ -25,7 +25,7 @@ def _snippet() -> str:
     text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     sec = text[text.index("## C++ (the reference's own language)"):]
     m = re.search(r"```cpp\n(.*?)```", sec, flags=re.S)
-    assert m, "no C++ block in INTEGRATION.md"
+    assert m, "no C++ block in the integration guide"
     return m.group(1)
 
 
@@ -64,7 +64,7 @@ TU = r"""
 #undef private
 #undef protected
 
-// ---- INTEGRATION.md ----
+// ---- the integration guide's C++ section ----
 %s
 // ------------------------
 
