@@ -73,13 +73,28 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams P) {
       else hi = mid - 1;
     }
   }
+  // the current domain and the tile's row and column, advanced tile by tile
+  // (a division only where the run enters a domain)
+  int     dom = -1, ty = 0, tx = 0;
+  int64_t next_start = 0;
   for(int64_t t = t0; t < t1; ++t) {
-    while(lo + 1 < na && P.tile_start[lo + 1] <= t) ++lo;
-    const BatchDomain D = P.dom[P.active[lo]];
-    const int64_t     r = t - P.tile_start[lo];
-    const int         y = static_cast<int>(r / D.tiles_per_row);
-    const int         x = static_cast<int>(r % D.tiles_per_row) * 32 + lane;
+    if(dom < 0 || t >= next_start) {
+      while(lo + 1 < na && P.tile_start[lo + 1] <= t) ++lo;
+      dom        = P.active[lo];
+      next_start = lo + 1 < na ? P.tile_start[lo + 1] : total;
+      const int64_t r   = t - P.tile_start[lo];
+      const int     tpr = P.dom[dom].tiles_per_row;
+      ty                = static_cast<int>(r / tpr);
+      tx                = static_cast<int>(r - static_cast<int64_t>(ty) * tpr);
+    }
+    const BatchDomain D = P.dom[dom];
+    const int         y = ty;
+    const int         x = tx * 32 + lane;
     const int         n = D.n;
+    if(++tx == D.tiles_per_row) {  // the next tile of this run
+      tx = 0;
+      ++ty;
+    }
     C                 diff[NV9] = {C(0), C(0), C(0)};  // summed in the arithmetic type, stored as FP64
     if(x < n) {
       T*            Ad   = A + D.pop_off;
