@@ -21,7 +21,11 @@
  *            12 significant bits, normal range [2^-14, 2), saturating;
  *          8 16-bit fixed point of s: round(s / S x 2^15) / 2^15, saturating;
           9 block floating point of s: per cell, 16-bit integers times one
-            power-of-two scale 2^(e - 15) with 2^e >= the cell's max |s|
+            power-of-two scale 2^(e - 15) with 2^e >= the cell's max |s|;
+          10 the same with the scale of the slot's owner, as the AA pattern
+            would hold it: set by the owner when it rewrites its own slots
+            (even steps, one bit of headroom), used by the values its
+            neighbours push into its slots (odd steps), saturating
  *   arith: 0 FP64 on v; 2 FP32 on the shifted state (the engine's
  *          single-precision collision in the same operation order)
  * out.bin: rho, ux, uy, uz per cell (FP64), x fastest.
@@ -79,6 +83,33 @@ static void store_block(double* x) {
   }
 }
 
+/* store 10: the same integers with the scale of the slot's owner cell: a cell
+   sets its exponent when it rewrites all its own slots (the even AA step,
+   from its post-collision values, `headroom` bits above their maximum), and
+   values pushed into its slots in the odd step use it, saturating */
+static void round_with(double* x, int e) {
+  const double sc = ldexp(1.0, e - 15);
+  for(int q = 0; q < 19; ++q) {
+    double v = nearbyint(x[q] / sc);
+    if(v > 32767) v = 32767;
+    if(v < -32767) v = -32767;
+    x[q] = v * sc;
+  }
+}
+static int store_owner(double* x, int headroom, double also) {
+  double m = also;
+  for(int q = 0; q < 19; ++q) m = fmax(m, fabs(x[q]));
+  int e = -10; /* a floor: a cell at the free stream (all values ~0) still takes what its neighbours push */
+  if(m > 0) {
+    int em;
+    frexp(m, &em);
+    if(em > e) e = em;
+  }
+  e += headroom;
+  round_with(x, e);
+  return e;
+}
+
 /* the stored value of x (state units: v or s) of direction q, cell i, step t */
 static double store(double x, int q, uint32_t i, uint32_t t) {
   switch(smode) {
@@ -121,6 +152,7 @@ int main(int argc, char** argv) {
   const char* out    = argv[12];
   const double om = 1.0 / tau, u0 = 0.05, S = 4096.0;
   const int    shifted = smode != 0 && smode != 2;
+  if(smode == 10 && steps % 2) fprintf(stderr, "store 10: an even number of steps ends on a full rewrite\n");
   const double U       = shifted ? u0 : 0.0;
   for(int q = 0; q < 19; ++q) {
     const int n2 = C[q][0] * C[q][0] + C[q][1] * C[q][1] + C[q][2] * C[q][2];
@@ -169,6 +201,7 @@ int main(int argc, char** argv) {
       }
   double* f  = malloc(sizeof(double) * 19 * N);
   double* fs = malloc(sizeof(double) * 19 * N);
+  int*    ex = calloc(N, sizeof(int)); /* store 10: the slot owner's exponent */
   double  feq0[19];
   for(int q = 0; q < 19; ++q) {
     const double cu = C[q][0] * u0;
@@ -238,7 +271,17 @@ int main(int argc, char** argv) {
         }
       }
       if(smode == 9) store_block(o);
-      for(int q = 0; q < 19; ++q) fs[q * N + i] = smode == 9 ? o[q] : store(o[q], q, (uint32_t)i, (uint32_t)t);
+      if(smode == 10 && (t & 1) == 0) {
+        /* even step: the cell rewrites its own slots; its exponent must also
+           hold what a bounce will put there (its own population of the
+           opposite direction plus the change of shift) */
+        double bmax = 0;
+        for(int k = 0; k < 19; ++k)
+          if(src[k * N + i] < 0) bmax = fmax(bmax, fabs(o[OPP[k]] + K[OPP[k]] - K[k]));
+        ex[i] = store_owner(o, 1, bmax);
+      }
+      for(int q = 0; q < 19; ++q)
+        fs[q * N + i] = (smode == 9 || smode == 10) ? o[q] : store(o[q], q, (uint32_t)i, (uint32_t)t);
     }
 #pragma omp parallel for schedule(static)
     for(int64_t i = 0; i < N; ++i) {
@@ -251,6 +294,14 @@ int main(int argc, char** argv) {
         const int64_t sidx = src[k * N + i];
         if(sidx >= 0) f[k * N + i] = fs[sidx];
         else f[k * N + i] = fs[-sidx - 1] + K[OPP[k]] - K[k]; /* bounced: the change of shift, added unrounded */
+      }
+      /* odd step: the values pushed into this cell's slots take its exponent
+         from the last even step (saturating where they exceed it) */
+      if(smode == 10 && (t & 1) == 1) {
+        double v[19];
+        for(int k = 0; k < 19; ++k) v[k] = f[k * N + i];
+        round_with(v, ex[i]);
+        for(int k = 0; k < 19; ++k) f[k * N + i] = v[k];
       }
     }
   }
