@@ -65,6 +65,12 @@ int lbm_nn_conv_uses_tc(const void* x, int ldx, const void* w, const void* y, in
 /* synchronises the stream; -6 (a bounded pipeline wait of a tensor-core convolution ran out since the last
  * call) or 0, and clears the flag */
 int lbm_nn_conv_status(void* stream);
+/* TEST ONLY.  The tensor-core convolution's pipeline waits are bounded (0.2 s each); when one runs out the
+ * CTA records the flag lbm_nn_conv_status reports, lets its copies and MMAs in flight complete, frees its
+ * tensor memory and returns (its output is then invalid).  This sets the limit (1 ns .. 0.5 s) and, with
+ * starve = 1, leaves every CTA's first K chunk unloaded, so the waits on it run out: a device-side timeout
+ * without a fault.  limit 200000000 and starve 0 restore the defaults. */
+int lbm_nn_conv_test_wait(int64_t limit_ns, int32_t starve);
 
 #ifdef __cplusplus
 }

@@ -54,6 +54,8 @@ struct ConvTc {
   int          wb, hb;      // TMA box: Wb pixels x Hb rows = 128
   int          cin_chunks;  // cin / 32
   int          nchunk;      // 9 cin / 32
+  uint64_t     limit_ns;    // limit of each pipeline wait
+  int          starve;      // test only: the first chunk is never loaded, so the waits on it run out
 };
 
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint32_t bar) {
@@ -170,10 +172,11 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const __grid_constant__ CU
     for(; kc < a.nchunk; ++kc) {
       const int      s  = kc % kStages;
       const uint32_t st = base + s * sbyte;
-      if(kc >= kStages && !mbar_wait_bounded(bars + 8 * (kStages + s), ((kc / kStages) - 1) & 1, kWaitNs)) {
+      if(kc >= kStages && !mbar_wait_bounded(bars + 8 * (kStages + s), ((kc / kStages) - 1) & 1, a.limit_ns)) {
         ok = false;
         break;
       }
+      if(a.starve && kc == 0) continue;  // test only: nothing arms this stage
       const int tap = kc / a.cin_chunks, cc = kc - tap * a.cin_chunks;
       const int dy = tap / 3 - 1, dx = tap - (tap / 3) * 3 - 1;
       mbar_expect_tx(bars + 8 * s, sbyte);
@@ -183,6 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const __grid_constant__ CU
     // every load issued lands before the CTA may leave
     for(int s = 0; s < kStages && s < kc; ++s) {
       const int last = s + ((kc - 1 - s) / kStages) * kStages;  // the last chunk issued into stage s
+      if(a.starve && last == 0) continue;                        // never issued
       if(!mbar_wait_bounded(bars + 8 * s, (last / kStages) & 1, kDrainLimitNs)) ok = false;
     }
   } else if(threadIdx.x == 32) {
@@ -191,7 +195,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const __grid_constant__ CU
     for(int kc = 0; kc < a.nchunk; ++kc) {
       const int      s  = kc % kStages;
       const uint32_t st = base + s * sbyte;
-      if(!mbar_wait_bounded(bars + 8 * s, (kc / kStages) & 1, kWaitNs)) {
+      if(!mbar_wait_bounded(bars + 8 * s, (kc / kStages) & 1, a.limit_ns)) {
         ok = false;
         break;
       }
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const __grid_constant__ CU
 
   // epilogue: warp w owns TMEM lanes 32 w .. 32 w + 31 (pixels of the tile)
   // warp-uniform, as the TMEM loads below are warp-collective
-  const bool have = __all_sync(0xffffffffu, mbar_wait_bounded(done, 0, 2 * kWaitNs + kDrainLimitNs));
+  const bool have = __all_sync(0xffffffffu, mbar_wait_bounded(done, 0, 2 * a.limit_ns + kDrainLimitNs));
   tc_fence_after();
   if(!have) ok = false;
   if(have) {
@@ -264,7 +268,9 @@ EncodeTiled encoder() {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
-int g_conv_path = 0;  // 0: tensor-core kernel where the shape qualifies; 1: never
+int      g_conv_path     = 0;        // 0: tensor-core kernel where the shape qualifies; 1: never
+uint64_t g_conv_limit_ns = kWaitNs;  // pipeline wait limit (lbm_nn_conv_test_wait)
+int      g_conv_starve   = 0;
 
 }  // namespace
 
@@ -304,7 +310,7 @@ int conv_tc_launch(const void* x, int ldx, const void* w, const float* bias, voi
            CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return -1;
   }
-  ConvTc a{bias, y, ldy, offy, H, W, cout, wb, hb, cin / kChunkK, 9 * cin / kChunkK};
+  ConvTc a{bias, y, ldy, offy, H, W, cout, wb, hb, cin / kChunkK, 9 * cin / kChunkK, g_conv_limit_ns, g_conv_starve};
   const int64_t tiles = static_cast<int64_t>(B) * H * W / kTileM;
   const size_t  smem  = smem_bytes(cout);
   auto          kern  = relu ? (out_f32 ? k_conv_tc<true, true> : k_conv_tc<true, false>)
@@ -321,6 +327,13 @@ extern "C" {
 int lbm_nn_set_conv_path(int path) {
   if(path != 0 && path != 1) return -1;
   lbm::g_conv_path = path;
+  return 0;
+}
+
+int lbm_nn_conv_test_wait(int64_t limit_ns, int32_t starve) {
+  if(limit_ns <= 0 || limit_ns > 500000000 || (starve != 0 && starve != 1)) return -1;
+  lbm::g_conv_limit_ns = static_cast<uint64_t>(limit_ns);
+  lbm::g_conv_starve   = starve;
   return 0;
 }
 

@@ -59,6 +59,7 @@ _NN = {
     "lbm_nn_conv_uses_tc": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                             C.c_int],
     "lbm_nn_conv_status": [C.c_void_p],
+    "lbm_nn_conv_test_wait": [C.c_int64, C.c_int32],
 }
 
 

@@ -125,3 +125,34 @@ def test_shapes_outside_the_tensor_core_kernel_fall_back():
     uses, y, ref = _run(lib, (1, 4, 8, 32, 32, 64, 64, 0, True, False), 0)
     assert uses == 0
     assert np.all(np.abs(y - ref) <= 1e-5 * float(np.abs(ref).max()) + 2.0 ** -8 * np.abs(ref))
+
+
+def test_pipeline_wait_that_runs_out_reports_status_without_a_fault():
+    """With a 1 ms limit and every CTA's first K chunk left unloaded, the
+    tensor-core convolution's bounded waits run out: lbm_nn_conv_status
+    reports -6, and with the defaults restored the same call is correct
+    again (the context stayed usable)."""
+    import torch
+
+    lib = _lib()
+    dev = torch.device("cuda", 0)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    shape = SHAPES[2]
+    B, H, W, cin, ldx, cout, ldy, offy, relu, out_f32 = shape
+    x = torch.zeros((B, H, W, ldx), dtype=torch.bfloat16, device=dev)
+    w = torch.zeros((cout, 9 * cin), dtype=torch.bfloat16, device=dev)
+    b = torch.zeros(cout, dtype=torch.float32, device=dev)
+    y = torch.zeros((B, H, W, ldy), dtype=torch.bfloat16, device=dev)
+    assert lib.lbm_nn_conv_uses_tc(x.data_ptr(), ldx, w.data_ptr(), y.data_ptr(), ldy, offy, B, H, W, cin, cout, 0) == 1
+    assert lib.lbm_nn_conv_test_wait(1_000_000, 1) == 0
+    try:
+        assert lib.lbm_nn_conv3x3_fwd(x.data_ptr(), ldx, w.data_ptr(), b.data_ptr(), y.data_ptr(), ldy, offy, B, H, W, cin, cout,
+                                      int(relu), 0, stream) == 0
+        assert lib.lbm_nn_conv_status(stream) == -6
+    finally:
+        assert lib.lbm_nn_conv_test_wait(200_000_000, 0) == 0
+    assert lib.lbm_nn_conv_test_wait(0, 0) == -1 and lib.lbm_nn_conv_test_wait(1000, 2) == -1
+    uses, out, ref = _run(lib, shape, 0)
+    assert uses == 1
+    got = out[..., offy:offy + cout]
+    assert np.all(np.abs(got - ref) <= 1e-5 * float(np.abs(ref).max()) + 2.0 ** -8 * np.abs(ref))
