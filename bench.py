@@ -220,8 +220,13 @@ def accuracy_run(args):
            "dtype": "f64 reference; f32 / f16 / bf16 storage with f32 arithmetic", "data": "synthetic", "rows": []}
     spec = {"f64": ("f64", True), "f32": ("f32", True), "f32_noshift": ("f32", False), "f16dev": ("f16dev", True),
             "f16dev_noshift": ("f16dev", False), "bf16dev": ("bf16dev", True)}
-    for (nx, ny, nz, r, c), checkpoints in (((256, 128, 128, 12.0, (64.0, 64.0, 64.0)), (1000, 5000, 20000, 50000)),
-                                           ((512, 256, 256, 24.0, (128.0, 128.0, 128.0)), (2000, 5000, 10000))):
+    runs = (((256, 128, 128, 12.0, (64.0, 64.0, 64.0)), (1000, 5000, 20000, 50000)),
+            ((512, 256, 256, 24.0, (128.0, 128.0, 128.0)), (2000, 5000, 10000)))
+    if args.acc_full_steps:
+        # the full box alone, to the given length (the configuration's 50,000)
+        full = sorted({c for c in (2000, 5000, 10000, 20000, 50000) if c < args.acc_full_steps} | {args.acc_full_steps})
+        runs = (((512, 256, 256, 24.0, (128.0, 128.0, 128.0)), tuple(full)),)
+    for (nx, ny, nz, r, c), checkpoints in runs:
         case = sphere_case(nx, ny, nz, radius=r, center=c)
         sol = {}
         for n, (st, sh) in spec.items():
@@ -243,6 +248,8 @@ def accuracy_run(args):
         for sv in sol.values():
             sv.close()
     out["value"] = next(r["f16dev"] for r in out["rows"] if r["case"] == "512x256x256" and r["steps"] == 5000)
+    if args.acc_full_steps:
+        out["value_at_end"] = out["rows"][-1]["f16dev"]
     out["config"] = {"workload": "D3Q19 flow past a sphere from the free stream; value: FP16 storage, full box, 5,000 steps",
                      "tau": sphere_case(64, 32, 32)["tau"]}
     return out
@@ -680,6 +687,7 @@ def main():
     ap.add_argument("--ws-lr", type=float, default=1e-3, help="warm start: peak learning rate")
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--cavity-check", type=int, default=1, help="cavities: also run a subset to convergence in FP64 and FP32 (1) or not (0)")
+    ap.add_argument("--acc-full-steps", type=int, default=0, help="accuracy: only the full 512x256x256 box, to this many steps")
     ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL) + ["cavities", "poisson", "unet"],
                     help="a small case for ncu captures, its measured launches inside the NVTX range 'profile': 4 steps of "
                          "a 256x128x128 version of the sphere workload in this storage; or 4 steps of 256 of the cavities; "
