@@ -155,29 +155,23 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
   return static_cast<int64_t>(q) * P.ny * P.nz + y + static_cast<int64_t>(P.ny) * z;
 }
 
-// The relaxation rate of z-slice z in the arithmetic type: the box's, or the
-// slice's where the box has one per slice.
-template <class C>
-__device__ __forceinline__ C slice_omega(const BoxParams& P, int z) {
-  if constexpr(sizeof(C) == 4) return P.slice_omega_f ? P.slice_omega_f[z] : P.omega_f;
-  else return P.slice_omega ? static_cast<C>(P.slice_omega[z]) : static_cast<C>(P.omega);
-}
-
-// The collision of one cell relaxing at rate om (Navier-Stokes; Poisson
-// boxes relax at the box's rate).  FP64 arithmetic (FP64 storage) works on
-// the scaled deviation v; FP32 arithmetic (the other storages) on the state
-// shifted to the free stream (collide_ns_shifted, U = P.shift_u).
+// The collision of one cell of z-slice z.  FP64 arithmetic (FP64 storage)
+// works on the scaled deviation v; FP32 arithmetic (the other storages) on
+// the state shifted to the free stream (collide_ns_shifted, U = P.shift_u).
+// The relaxation rate is the slice's where the box has one per slice.
 template <int LAT, int EQ, class C>
-__device__ __forceinline__ void collide_at(const BoxParams& P, C om, C* v, C* mom_out) {
+__device__ __forceinline__ void collide(const BoxParams& P, int z, C* v, C* mom_out) {
   if constexpr(EQ == LBM_NAVIER_STOKES) {
     C F[3];
     F[0] = prm<C>(P.force[0], P.force_f[0]);
     F[1] = prm<C>(P.force[1], P.force_f[1]);
     F[2] = prm<C>(P.force[2], P.force_f[2]);
     if constexpr(sizeof(C) == 4) {
+      const float om = P.slice_omega_f ? P.slice_omega_f[z] : P.omega_f;
       if(P.has_force) collide_ns_shifted<LAT, true>(om, true, F, P.shift_u, v, mom_out);
       else collide_ns_shifted<LAT, false>(om, false, F, P.shift_u, v, mom_out);
     } else {
+      const C om = P.slice_omega ? static_cast<C>(P.slice_omega[z]) : prm<C>(P.omega, P.omega_f);
       if(P.has_force) collide_ns<LAT, C, true>(om, true, F, v, mom_out);
       else collide_ns<LAT, C, false>(om, false, F, v, mom_out);
     }
@@ -185,12 +179,6 @@ __device__ __forceinline__ void collide_at(const BoxParams& P, C om, C* v, C* mo
     collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
                             mom_out);
   }
-}
-
-// The collision of one cell of z-slice z.
-template <int LAT, int EQ, class C>
-__device__ __forceinline__ void collide(const BoxParams& P, int z, C* v, C* mom_out) {
-  collide_at<LAT, EQ, C>(P, slice_omega<C>(P, z), v, mom_out);
 }
 
 // state emitted by inlet / Dirichlet cells

@@ -126,7 +126,7 @@ __device__ __forceinline__ void cp_async_elem(C* dst, const C* src) {
 // previous moments are at prev_s[v * kRowThreads], fetched with cp.async.
 template <int LAT, int EQ, int ST, bool ODD, int WR, int MOM, int NV>
 __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>::T* bx, int x, int y, int z, bool outlet_inline,
-                                         typename Store<ST>::C om, typename Store<ST>::C* dacc, const typename Store<ST>::C* prev_s) {
+                                         typename Store<ST>::C* dacc, const typename Store<ST>::C* prev_s) {
   using L         = Lattice<LAT>;
   using S         = Store<ST>;
   using T         = typename S::T;
@@ -159,7 +159,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
       if constexpr(ODD) f[q] = S::load(bx[L::opp(q) * WR - L::c(q, 0)]);
       else f[q] = S::load(bx[q * WR]);
     });
-    collide_at<LAT, EQ, C>(P, om, f, MOM ? mom : nullptr);
+    collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
   } else {
     const bool emit = ODD ? (special && type == LBM_CELL_INLET) : (type == LBM_CELL_INLET || type == LBM_CELL_DIRICHLET);
     if(emit) {
@@ -192,7 +192,7 @@ __device__ __forceinline__ void row_cell(const BoxParams& P, typename Store<ST>:
           });
         }
       }
-      collide_at<LAT, EQ, C>(P, om, f, MOM ? mom : nullptr);
+      collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
     }
     __syncwarp(active);  // every lane's staged reads come before any lane's stores
   }
@@ -353,11 +353,10 @@ __global__ void __launch_bounds__(kRowBlock, row_min_ctas<ST>()) k_box_rows(BoxP
       asm volatile("cp.async.commit_group;" ::: "memory");
     }
     {
-      const C om = slice_omega<C>(P, z);  // one rate per row
-      int     j  = 0;
+      int j = 0;
 #pragma unroll 1
       for(int x = tid; x < nx; x += kRowThreads, ++j)
-        row_cell<LAT, EQ, ST, ODD, WR, MOM, NV>(P, stage + x, x, y, z, R.outlet_inline != 0, om, dacc, prevbuf + j * 4 * kRowThreads + tid);
+        row_cell<LAT, EQ, ST, ODD, WR, MOM, NV>(P, stage + x, x, y, z, R.outlet_inline != 0, dacc, prevbuf + j * 4 * kRowThreads + tid);
     }
     if constexpr(MOM == 2) cp_async_wait_all();  // none left in flight (cells that did no work never waited)
     fence_async_smem();  // this thread's writes are visible to the bulk stores
