@@ -34,23 +34,23 @@ CASES = [
     ("couette", ("ref", "test/couette/couette.json"), [1, 50]),
     ("couette_bnd", ("ref", "test/couette/couette_bnd.json"), [1, 50]),
     ("couette_bnd_bbDirichlet", ("ref", "test/couette/couette_bnd_bbDirichlet.json"), [50]),
-    ("couette_bnd_eq", ("ref", "test/couette/couette_bnd_eq.json"), [50]),
+    ("couette_bnd_eq", ("ref", "test/couette/couette_bnd_eq.json"), [50, 1000]),
     ("couette_bnd_eq2", ("ref", "test/couette/couette_bnd_eq2.json"), [50]),
     ("couette_bnd_NEEM", ("ref", "test/couette/couette_bnd_NEEM.json"), [50, 1000]),
-    ("couette_bnd_NEBB", ("ref", "test/couette/couette_bnd_NEBB.json"), [50]),
+    ("couette_bnd_NEBB", ("ref", "test/couette/couette_bnd_NEBB.json"), [50, 1000]),
     ("poiseuille", ("ref", "test/poiseuille/poiseuille.json"), [1, 50, 1000]),
     ("poiseuille_bnd", ("ref", "test/poiseuille/poiseuille_bnd.json"), [50]),
     ("poiseuille_bnd_eq", ("ref", "test/poiseuille/poiseuille_bnd_eq.json"), [50]),
     ("poiseuille_bnd_NEEM", ("ref", "test/poiseuille/poiseuille_bnd_NEEM.json"), [50]),
     ("poiseuille_bnd_NEBB", ("ref", "test/poiseuille/poiseuille_bnd_NEBB.json"), [50]),
-    ("poiseuille_bnd_pressure", ("ref", "test/poiseuille/poiseuille_bnd_pressure.json"), [50]),
+    ("poiseuille_bnd_pressure", ("ref", "test/poiseuille/poiseuille_bnd_pressure.json"), [50, 1000]),
     ("poiseuille_bnd_pressure_neem2", ("ref", "test/poiseuille/poiseuille_bnd_pressure_neem2.json"), [50]),
     ("poisson1D_reaction", ("ref", "test/poisson/poisson1D_reaction.json"), [50, 1000]),
     ("poisson1d_dh_small", ("own", "poisson1d_dh_small.json"), [1, 100]),
     ("poisson2d_d2q5_small", ("own", "poisson2d_d2q5_small.json"), [1, 100]),
     ("poisson2d_d2q9_reaction_small", ("own", "poisson2d_d2q9_reaction_small.json"), [100]),
-    ("poisson2d_helmholtz_small", ("own", "poisson2d_helmholtz_small.json"), [100]),
-    ("cavity_small", ("own", "cavity_small.json"), [1, 100]),
+    ("poisson2d_helmholtz_small", ("own", "poisson2d_helmholtz_small.json"), [100, 1000]),
+    ("cavity_small", ("own", "cavity_small.json"), [1, 100, 1000]),
     ("channel_mixed_small", ("own", "channel_mixed_small.json"), [1, 100]),
     # the reference's remaining Poisson tests and its backward-facing steps
     # (bodies made of several boxes), at coarser levels
@@ -59,7 +59,7 @@ CASES = [
     ("poisson2D_reaction_l5", ("ref", "test/poisson/poisson2D_reaction.json",
                                {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [50]),
     ("poissonD2Q9_l5", ("ref", "test/poisson/poissonD2Q9.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [50]),
-    ("step_ns_l5", ("ref", "test/step/step_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [40]),
+    ("step_ns_l5", ("ref", "test/step/step_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [40, 1000]),
     ("step_poisson_l5", ("ref", "test/step/step_poisson.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}), [40]),
     # the reference's 2D flow around an obstacle (box minus a circle, pressure
     # inlet / outlet, bounce-back walls) at level 5 instead of 8
