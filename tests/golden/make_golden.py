@@ -31,7 +31,7 @@ REF = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), "--root"], c
 
 # (fixture name, config path, step counts)
 CASES = [
-    ("couette", ("ref", "test/couette/couette.json"), [1, 50]),
+    ("couette", ("ref", "test/couette/couette.json"), [1, 50, 1000]),
     ("couette_bnd", ("ref", "test/couette/couette_bnd.json"), [1, 50]),
     ("couette_bnd_bbDirichlet", ("ref", "test/couette/couette_bnd_bbDirichlet.json"), [50]),
     ("couette_bnd_eq", ("ref", "test/couette/couette_bnd_eq.json"), [50, 1000]),

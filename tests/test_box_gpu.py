@@ -33,7 +33,7 @@ def sphere_flags(shape, center, radius, inlet_outlet=True):
     return fl.reshape(-1)
 
 
-@pytest.mark.parametrize("name", ["couette_1", "couette_50"])
+@pytest.mark.parametrize("name", ["couette_1", "couette_50", "couette_1000"])
 def test_box_fp64_matches_reference_couette(name):
     meta, solver, grid, out, consts, bnds, forcing = load_case(name)
     ij, (nx, ny) = box_index(grid)

@@ -32,7 +32,7 @@ def couette_oracle(name, deviation):
     return o.populations()[:, idx].T, out["fold"].reshape(grid.ncells, 9)
 
 
-@pytest.mark.parametrize("name", ["couette_1", "couette_50"])
+@pytest.mark.parametrize("name", ["couette_1", "couette_50", "couette_1000"])
 @pytest.mark.parametrize("deviation", [False, True])
 def test_box_oracle_matches_reference_couette(name, deviation):
     f, ref = couette_oracle(name, deviation)
