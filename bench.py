@@ -550,9 +550,19 @@ def grid_run(args):
     t_host = time.perf_counter() - t0
     same = bool(np.array_equal(dev.centers, host.centers) and np.array_equal(dev.nghbr, host.nghbr) and
                 all(np.array_equal(dev.surfaces[k]["cells"], host.surfaces[k]["cells"]) for k in host.surfaces))
+    # the multi-level generator (host): a 2D channel minus a cylinder,
+    # partitioning level 4, uniform to level 10, boundary cells refined to 13
+    tree_cfg = {"dim": 2, "partitionLevel": 4, "uniformLevel": 10, "maxRfnmtLvl": 13, "maxNoCells": 20_000_000,
+                "geometry": {"cube": {"type": "box", "body": "flow", "A": [0.0, 0.0], "B": [10.0, 4.0]},
+                             "cyl": {"type": "sphere", "body": "flow", "subtract": True, "center": [3.1, 2.05], "radius": 0.8}}}
+    t0 = time.perf_counter()
+    tree = gridgen.grid_tree(tree_cfg)
+    t_tree = time.perf_counter() - t0
     return {"metric": "grid and table build, D3Q19 sphere channel 512x256x256 from its JSON config", "value": t_dev, "unit": "s",
             "higher_is_better": False, "config": {"workload": "uniform level 9, box minus sphere r=24", "cells": dev.ncells},
-            "host_s": t_host, "device_s": t_dev, "identical": same}
+            "host_s": t_host, "device_s": t_dev, "identical": same,
+            "tree": {"workload": "2D channel minus cylinder, partitioning level 4, uniform to 10, boundary-refined to 13 (host)",
+                     "cells": int(len(tree.level)), "levels": [tree.partition_level, tree.highest_level], "s": t_tree}}
 
 
 def lpt_run(args):

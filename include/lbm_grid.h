@@ -118,6 +118,49 @@ int lbm_grid_connect_periodic(lbm_grid* g, const int64_t* cells_a, int64_t na, c
 int lbm_grid_neighbors(const lbm_grid* g, int64_t* out);
 void lbm_grid_destroy(lbm_grid* g);
 
+/* ---- Multi-level grids: the reference generator's whole cell tree ------ */
+
+typedef struct lbm_grid_tree lbm_grid_tree;
+
+/* columns of lbm_grid_tree_write_points ("outputValues") */
+#define LBM_TREE_COLUMN_LEVEL 0
+#define LBM_TREE_COLUMN_NOCHILDREN 1
+
+/* The cell tree GridGenerator::generateGrid builds
+ * (src/gridgenerator/gridGenerator.cpp:163-238,
+ * src/gridgenerator/cartesiangrid_generation.h) for
+ * 0 <= partition_level <= uniform_level <= max_level <= 20 in an array of
+ * max_cells slots ("maxNoCells"): the partitioning level in curve order
+ * (createPartitioningGrid, :71-147), every cell refined up to uniform_level
+ * (uniformRefineGrid, :151-169), then the boundary cells of the finest level
+ * refined up to max_level (markBndryCells / refineMarkedCells, :173-206),
+ * each new level appended after the grid with its outside cells deleted in
+ * the reference's order.  align_dir >= 0 applies alignNodesWithSurface along
+ * that axis to the cells of max_level (:255-304); -1 skips it.  The cells are
+ * those of the reference's array, in its order: the partitioning level first,
+ * then each finer level.  LBM_ERR_NOMEM: the grid does not fit in max_cells
+ * slots (the reference stops with "Out of memory"). */
+int lbm_grid_tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_level, int32_t max_level, int64_t max_cells,
+                         const lbm_geom_desc* objs, int32_t nobj, const double* bbox, int32_t align_dir, lbm_grid_tree** out);
+int64_t lbm_grid_tree_ncells(const lbm_grid_tree* t);
+/* partitioning level and the finest level built */
+int lbm_grid_tree_levels(const lbm_grid_tree* t, int32_t* partition_level, int32_t* highest_level);
+/* per cell (any pointer may be NULL): centres (ncells x ndim), level, parent
+ * (-1: none), global id (the slot the cell was created in), number of
+ * children, boundary property */
+int lbm_grid_tree_cells(const lbm_grid_tree* t, double* centers, int8_t* level, int64_t* parent, int64_t* global_id, int32_t* nchildren,
+                        uint8_t* bndry);
+/* child ids, ncells x 2^ndim in child order (bit d set: the + half along
+ * axis d), -1: none */
+int lbm_grid_tree_children(const lbm_grid_tree* t, int64_t* out);
+/* same-level neighbours, ncells x 2 ndim (-x, +x, -y, +y, -z, +z), -1: none */
+int lbm_grid_tree_neighbors(const lbm_grid_tree* t, int64_t* out);
+/* the generator's points file (ASCII::writePointsCSV, src/common/IO.h:36-81):
+ * a header of the axis names and the columns, then one line per cell with
+ * the centre at 15 significant digits and the listed columns */
+int lbm_grid_tree_write_points(const lbm_grid_tree* t, const char* path, const int32_t* columns, int32_t ncolumns);
+void lbm_grid_tree_destroy(lbm_grid_tree* t);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,8 @@ UNITS = {
     # host-only grid and table build: no floating-point contraction, so that
     # the cut tests round as the reference's do on either host architecture
     "grid.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    # the multi-level generator (same geometry code, same rule)
+    "grid_tree.cpp": ["-Xcompiler", "-ffp-contract=off"],
     # its device counterpart: the same geometry code, no contraction either
     "grid_device.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # particle step: the reference's separately rounded FP64 operations

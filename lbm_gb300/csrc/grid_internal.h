@@ -43,4 +43,6 @@ int setup(lbm_grid& g, int ndim, int level, const lbm_geom_desc* objs, int nobj,
 void link_cells(lbm_grid& g);
 // boundary-cell list from the boundary property
 void list_boundary_cells(lbm_grid& g);
+// hilbert::index (include/common/math/hilbert.h:16-48) of a point of the unit cube
+uint64_t curve_index(const double* x, int D, int level);
 }  // namespace lbm_grid_impl

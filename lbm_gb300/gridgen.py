@@ -29,10 +29,16 @@ config in the reference's order:
 
 In 2D and 1D the tables equal the reference's bit for bit; 3D, which the
 reference cannot build, follows the same rules (include/lbm_grid.h).
+
+:func:`grid_tree` builds the generator's whole multi-level cell tree for any
+``partitionLevel <= uniformLevel <= maxRfnmtLvl`` (``lbm_grid_tree_create``),
+and :func:`save_grid` writes the generator's points file from it.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
+from dataclasses import dataclass
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -66,6 +72,15 @@ _SIGS = {
     "lbm_grid_connect_periodic": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]),
     "lbm_grid_neighbors": (C.c_int, [C.c_void_p, C.c_void_p]),
     "lbm_grid_destroy": (None, [C.c_void_p]),
+    "lbm_grid_tree_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
+                                       C.c_int32, C.POINTER(C.c_void_p)]),
+    "lbm_grid_tree_ncells": (C.c_int64, [C.c_void_p]),
+    "lbm_grid_tree_levels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "lbm_grid_tree_cells": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "lbm_grid_tree_children": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_grid_tree_neighbors": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_grid_tree_write_points": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int32]),
+    "lbm_grid_tree_destroy": (None, [C.c_void_p]),
 }
 
 
@@ -130,7 +145,11 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
     levels = {k: int(config[k]) for k in ("partitionLevel", "uniformLevel", "maxRfnmtLvl") if k in config}
     level = levels.get("uniformLevel", levels.get("partitionLevel"))
     if level is None or len(set(levels.values())) != 1:
-        raise ConfigError("only uniform grids are built: partitionLevel, uniformLevel and maxRfnmtLvl must be equal")
+        # the reference's solver would step every level of a multi-level
+        # array as a lattice of its own (src/lbm/solver.cpp:525); the
+        # generator's tree for such a config is grid_tree's
+        raise ConfigError("the LBM tables are built for uniform grids: partitionLevel, uniformLevel and maxRfnmtLvl must be "
+                          "equal (grid_tree builds the generator's multi-level tree)")
     geometry = config.get("geometry", {})
     descs, names = geometry_objects(geometry, ndim)
     bbox = None
@@ -214,6 +233,110 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
         lib.lbm_grid_destroy(h)
     return GridTables(ndim=ndim, centers=centers, nghbr=nghbr, surfaces=surfaces, bbox=box, cell_length=float(cl.value),
                       max_lvl=level)
+
+
+@dataclass
+class GridTree:
+    """The reference grid generator's cell array (all levels, its order)."""
+    ndim: int
+    partition_level: int
+    highest_level: int
+    centers: np.ndarray    # (n, ndim)
+    level: np.ndarray      # (n,) int8
+    parent: np.ndarray     # (n,) int64, -1: none
+    global_id: np.ndarray  # (n,) int64
+    nchildren: np.ndarray  # (n,) int32
+    bndry: np.ndarray      # (n,) uint8
+    children: np.ndarray   # (n, 2**ndim) int64, -1: none
+    nghbr: np.ndarray      # (n, 2*ndim) int64, -1: none
+
+    def leaves(self) -> np.ndarray:
+        """Cells without children (the reference's "leafCells" filter)."""
+        return np.flatnonzero(self.nchildren == 0)
+
+
+# GridGenerator's "outputValues" (src/gridgenerator/cartesiangrid_generation.h:224-240)
+TREE_COLUMNS = {"level": 0, "noChildren": 1}
+
+
+def _tree_levels(config: Dict):
+    """partitionLevel, uniformLevel, maxRfnmtLvl and maxNoCells with the
+    generator's checks (src/gridgenerator/gridGenerator.cpp:245-255, 130-133)."""
+    for key in ("partitionLevel", "uniformLevel", "maxNoCells"):
+        if key not in config:
+            raise ConfigError(f'"{key}" is required')
+    p, u = int(config["partitionLevel"]), int(config["uniformLevel"])
+    m = int(config.get("maxRfnmtLvl", u))
+    if p > u:
+        raise ConfigError("Invalid definition of grid level partitionLevel >= uniformLevel")
+    if m < u:
+        raise ConfigError("Invalid definition of grid level uniformLevel >= maxRfnmtLvl")
+    return p, u, m, int(config["maxNoCells"])
+
+
+def grid_tree(config: Dict, points_file: Optional[str] = None) -> GridTree:
+    """The reference grid generator's whole cell tree for a JSON config (its
+    keys: ``dim``, ``partitionLevel``, ``uniformLevel``, ``maxRfnmtLvl``,
+    ``maxNoCells``, ``geometry``, ``boundingBox``, ``alignNodesWithSurface``,
+    ``alignDir``), built natively (``lbm_grid_tree_create``).  With
+    ``points_file`` the generator's points file is written there too, with
+    the columns of ``output.outputValues`` (default ``["level"]``)."""
+    ndim = int(config.get("dim", 0))
+    if ndim not in (1, 2, 3):
+        raise ConfigError(f"dim must be 1, 2 or 3, got {ndim}")
+    p, u, m, cap = _tree_levels(config)
+    descs, names = geometry_objects(config.get("geometry", {}), ndim)
+    bbox = None
+    if not names or "boundingBox" in config:
+        bbox = (C.c_double * (2 * ndim))(*[float(x) for x in config.get("boundingBox", [0.0, 1.0] * ndim)])
+    align = int(config.get("alignDir", 1)) if config.get("alignNodesWithSurface", False) else -1
+    lib = _grid_lib()
+    h = C.c_void_p()
+    _lib.check(lib.lbm_grid_tree_create(ndim, p, u, m, cap, C.cast(descs, C.c_void_p), len(names),
+                                        C.cast(bbox, C.c_void_p) if bbox else None, align, C.byref(h)),
+               what="lbm_grid_tree_create")
+    try:
+        n = int(lib.lbm_grid_tree_ncells(h))
+        pl, hl = C.c_int32(), C.c_int32()
+        _lib.check(lib.lbm_grid_tree_levels(h, C.byref(pl), C.byref(hl)), what="lbm_grid_tree_levels")
+        t = GridTree(ndim=ndim, partition_level=int(pl.value), highest_level=int(hl.value),
+                     centers=np.empty((n, ndim)), level=np.empty(n, np.int8), parent=np.empty(n, np.int64),
+                     global_id=np.empty(n, np.int64), nchildren=np.empty(n, np.int32), bndry=np.empty(n, np.uint8),
+                     children=np.empty((n, 1 << ndim), np.int64), nghbr=np.empty((n, 2 * ndim), np.int64))
+        _lib.check(lib.lbm_grid_tree_cells(h, t.centers.ctypes.data, t.level.ctypes.data, t.parent.ctypes.data,
+                                           t.global_id.ctypes.data, t.nchildren.ctypes.data, t.bndry.ctypes.data),
+                   what="lbm_grid_tree_cells")
+        _lib.check(lib.lbm_grid_tree_children(h, t.children.ctypes.data), what="lbm_grid_tree_children")
+        _lib.check(lib.lbm_grid_tree_neighbors(h, t.nghbr.ctypes.data), what="lbm_grid_tree_neighbors")
+        if points_file is not None:
+            values = config.get("output", {}).get("outputValues", ["level"])
+            cols = [TREE_COLUMNS[v] for v in values if v in TREE_COLUMNS]  # the reference skips unknown values
+            arr = (C.c_int32 * max(1, len(cols)))(*cols)
+            _lib.check(lib.lbm_grid_tree_write_points(h, os.fsencode(points_file), C.cast(arr, C.c_void_p), len(cols)),
+                       what="lbm_grid_tree_write_points")
+    finally:
+        lib.lbm_grid_tree_destroy(h)
+    return t
+
+
+def save_grid(config: Dict, workdir: str = ".") -> str:
+    """GridGenerator::run's output: the tree's points file at
+    ``<workdir>/<outputDir>/<gridFileName>.csv`` (defaults ``out`` and
+    ``grid``; the directory must exist, as the reference requires).  Only the
+    ASCII format is written; the reference's VTK point writers stop with
+    "Work in progress" (src/common/IO.h:219).  Every cell is written whatever
+    ``cellFilter`` says: the generator builds its filter without the grid, so
+    it passes all cells (src/gridgenerator/cartesiangrid_generation.h:220,
+    src/cell_filter.h:62)."""
+    out = config.get("output", {"format": "ASCII"})
+    if out.get("format", "ASCII") != "ASCII":
+        raise ConfigError(f'grid output format "{out.get("format")}" is not written (the reference stops on it too)')
+    outdir = os.path.join(workdir, config.get("outputDir", "out"))
+    if not os.path.isdir(outdir):
+        raise ConfigError(f"Is not a valid output directory! {outdir}")
+    path = os.path.join(outdir, config.get("gridFileName", "grid") + ".csv")
+    grid_tree(config, points_file=path)
+    return path
 
 
 # box-engine face kinds for the reference's boundary types, plus the kinds the

@@ -15,7 +15,9 @@
 #      placeholders filled in;
 #   3. compile the reference's grid generator TU and oracle/ref_harness.cpp
 #      (which includes src/lbm/solver.cpp) against a serial MPI stub
-#      (oracle/mpi_stub/mpi.h), and link oracle/_ref/ref_harness.
+#      (oracle/mpi_stub/mpi.h), and link oracle/_ref/ref_harness; link the
+#      same generator TU with oracle/ref_gridgen_harness.cpp into
+#      oracle/_ref/ref_gridgen_harness (the generator's cell tree).
 #
 # Usage: oracle/build_ref.sh [reference_root]
 #        oracle/build_ref.sh --root     print the reference root it would use
@@ -60,9 +62,13 @@ P1=$!
 P2=$!
 "$CXX" "${FLAGS[@]}" -c "$HERE/ref_lpt_harness.cpp" -o "$OUT/ref_lpt_harness.o" &
 P3=$!
+"$CXX" "${FLAGS[@]}" -c "$HERE/ref_gridgen_harness.cpp" -o "$OUT/ref_gridgen_harness.o" &
+P4=$!
 wait $P1
 wait $P2
 wait $P3
+wait $P4
 "$CXX" -fopenmp "$OUT/gridGenerator.o" "$OUT/ref_harness.o" -o "$OUT/ref_harness" -ldl -lpthread
 "$CXX" -fopenmp "$OUT/ref_lpt_harness.o" -o "$OUT/ref_lpt_harness" -ldl -lpthread
-echo "built $OUT/ref_harness $OUT/ref_lpt_harness"
+"$CXX" -fopenmp "$OUT/gridGenerator.o" "$OUT/ref_gridgen_harness.o" -o "$OUT/ref_gridgen_harness" -ldl -lpthread
+echo "built $OUT/ref_harness $OUT/ref_lpt_harness $OUT/ref_gridgen_harness"

@@ -23,8 +23,9 @@ def fixture_path(name: str) -> str:
 
 
 def list_fixtures():
-    """The LBM fixtures (the particle solver's are lpt_*)."""
-    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz") and not f.startswith("lpt_"))
+    """The LBM fixtures (the particle solver's are lpt_*, the grid
+    generator's gridtree_*)."""
+    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz") and not f.startswith(("lpt_", "gridtree_")))
 
 
 def list_lpt_fixtures():
