@@ -477,6 +477,54 @@ def sweep_run(args):
             "slices_bitwise_vs_own_boxes_after_100_steps": same}
 
 
+def debye_run(args):
+    """A Debye-length sweep stepped by one launch per step: 8 charged-sphere
+    boxes 128^3 (Debye length 4-32 and 1-64 spheres by seed, potential 0 on
+    each box's outer layer) stacked along z into one D3Q7 box 128x128x1024,
+    each box at its own kappa^2, nonlinear sinh source, FP32 storage.
+    Device-timed steps and the HBM fraction; then three boxes checked bit for
+    bit against boxes of their own after 60 steps."""
+    from lbm_gb300 import cases
+    from lbm_gb300.solver import BoxSolver
+
+    n_box, n = 8, 128
+    units = [cases.pb_spheres(n, seed=s) for s in range(n_box)]
+    st = cases.stacked_debye(units)
+    g = BoxSolver(st["lattice"], st["shape"], st["omega"], "f32", pb_nonlinear=True, **cases.box_kwargs(st))
+    g.set_slice_kappa(st["slice_kappa_sq"])
+    g.initial_condition()
+    g.step(args.warmup)
+    tot, ker, nl = g.profile_steps(args.steps)
+    cells = n * n * n * n_box
+    bpc = 2 * 7 * 4 + 1
+    hbm, peak_kind = peaks()
+    ach = bpc * cells / (ker / nl / 1e3) / 1e9
+    g.initial_condition()
+    g.step(60)
+    f = g.populations()
+    same = {}
+    for k in (0, n_box // 2, n_box - 1):
+        u = units[k]
+        s1 = BoxSolver(u["lattice"], u["shape"], u["omega"], "f32", pb_nonlinear=True, **cases.box_kwargs(u))
+        s1.initial_condition()
+        s1.step(60)
+        same[str(k)] = bool(np.array_equal(f[:, k * n ** 3:(k + 1) * n ** 3], s1.populations()))
+        s1.close()
+    kernel = g.kernel()
+    g.close()
+    debye = [u["debye"] for u in units]
+    return {"metric": "MLUPS (Debye-length sweep: 8 D3Q7 Poisson-Boltzmann boxes 128^3, FP32, one launch per step)",
+            "value": cells * args.steps / (tot / 1e3) / 1e6, "unit": "MLUPS", "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot / args.steps, "dtype": "f32", "higher_is_better": True,
+            "config": {"workload": "8 charged-sphere boxes 128^3 stacked along z, Debye length 4-32 and 1-64 spheres by seed, "
+                                   "one kappa^2 per box", "cells": cells, "bytes_per_cell": bpc,
+                       "debye_min_max": [min(debye), max(debye)], "spheres": [len(u["spheres"]) for u in units],
+                       "bulk_kernel": kernel},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "peak_kind": peak_kind,
+                         "kernel_avg_ms": ker / nl},
+            "boxes_bitwise_vs_own_boxes_after_60_steps": same}
+
+
 def poiseuille_run(args):
     """D2Q9 Guo-forced Poiseuille channel 256x64, plain FP64, 20,000 steps
     (the state fits in L2): device-timed MLUPS and the deviation from the
@@ -687,7 +735,7 @@ def main():
     ap.add_argument("--storage", default="f16dev", choices=list(B_PER_CELL))
     ap.add_argument("--quick", action="store_true", help="skip the FP32/BF16 comparison runs")
     ap.add_argument("--workload", default="sphere",
-                    choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt", "accuracy", "sweep"],
+                    choices=["sphere", "cavities", "poisson", "poiseuille", "warmstart", "grid", "lpt", "accuracy", "sweep", "debye"],
                     help="the headline sphere workload, or one of the other configurations (one JSON line each)")
     ap.add_argument("--max-steps", type=int, default=400000, help="step bound of the Poisson-Boltzmann and warm-start solves")
     ap.add_argument("--ws-train", type=int, default=1024, help="warm start: training channels")
@@ -729,7 +777,8 @@ def main():
     if args.workload != "sphere":
         if int(os.environ.get("RANK", "0")) == 0:
             fn = {"cavities": cavities_run, "poisson": poisson_run, "poiseuille": poiseuille_run, "warmstart": warmstart_run,
-                  "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run, "sweep": sweep_run}[args.workload]
+                  "grid": grid_run, "lpt": lpt_run, "accuracy": accuracy_run, "sweep": sweep_run,
+                  "debye": debye_run}[args.workload]
             # clocks sampled over the whole workload run (set-up included)
             with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
                 line = fn(args)

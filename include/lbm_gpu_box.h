@@ -136,6 +136,16 @@ int lbm_gpu_box_kernels(lbm_gpu_ctx* ctx, int32_t* even, int32_t* odd);
  * counterpart there.  LBM_ERR_UNSUPPORTED for Poisson boxes. */
 int lbm_gpu_box_set_slice_omega(lbm_gpu_ctx* ctx, const double* omega, int32_t n);
 
+/* Poisson-Boltzmann boxes: a kappa^2 per z-slice (kappa_sq[z] >= 0, n = nz
+ * values), so that boxes stacked along z, each closed by planes of
+ * LBM_CELL_DIRICHLET cells (which emit their own equilibrium whatever they
+ * receive), are a sweep over Debye length 1/kappa (and charge placement)
+ * stepped by one launch per step; kappa_sq = NULL restores the box's
+ * single kappa^2.  Each stacked box then steps exactly as a box of its own
+ * with its kappa^2.  Like the rate sweep, this has no counterpart in the
+ * reference.  LBM_ERR_UNSUPPORTED for Navier-Stokes boxes. */
+int lbm_gpu_box_set_slice_kappa(lbm_gpu_ctx* ctx, const double* kappa_sq, int32_t n);
+
 /* TEST ONLY.  The staged kernels' (LBM_BOX_KERNEL_STAGED and
  * LBM_BOX_KERNEL_ROWS) pipeline waits are bounded (0.5 s each);
  * when one runs out the kernel records a flag, lets its copies in flight

@@ -80,6 +80,7 @@ _SIGS = {
     "lbm_gpu_box_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "lbm_gpu_box_test_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
     "lbm_gpu_box_set_slice_omega": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "lbm_gpu_box_set_slice_kappa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "lbm_gpu_box_storage_bytes": (C.c_int, [C.c_int32]),
     "lbm_gpu_create_batch": (C.c_int, [C.POINTER(BatchDesc), C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "lbm_gpu_batch_residuals": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -67,7 +67,7 @@ def pb_spheres(n: int = 256, seed: int = 7, count: int | None = None, tau: float
     tries = 0
     while len(spheres) < count and tries < 100000:
         tries += 1
-        r = float(rng.uniform(4.0, 16.0))
+        r = float(rng.uniform(4.0, min(16.0, (n - 6) / 2.0)))  # radius 4-16, smaller in a box below 38 cells
         c = rng.uniform(r + 2, n - r - 2, size=3)
         if all(np.linalg.norm(c - c2) > r + r2 + 2 for c2, r2, _ in spheres):
             spheres.append((c, r, float(rng.uniform(0.5, 4.0))))
@@ -172,6 +172,30 @@ def stacked_sweep(cases_: List[Dict]) -> Dict:
     return dict(lattice=D2Q9, shape=(nx, ny, len(cases_)), omega=1.0 / cases_[0]["tau"], flags=flags,
                 faces=("open", "open", "wall", "wall", "periodic", "periodic"), inlet_velocity=(u_in, 0.0, 0.0),
                 slice_omega=[1.0 / c["tau"] for c in cases_])
+
+
+def stacked_debye(cases_: List[Dict]) -> Dict:
+    """Poisson-Boltzmann boxes (pb_spheres) of any Debye lengths and charge
+    placements stacked along z into one D3Q7 box: a sweep over Debye length
+    stepped together, each box's slices at its own kappa^2 (`slice_kappa_sq`,
+    for BoxSolver.set_slice_kappa).  Each box keeps its outer layer of
+    Dirichlet cells, so the boxes do not exchange populations.  All boxes
+    share nx, ny and the relaxation rate."""
+    nx, ny, _ = cases_[0]["shape"]
+    omega = cases_[0]["omega"]
+    if any(tuple(c["shape"][:2]) != (nx, ny) or c["omega"] != omega for c in cases_):
+        raise ValueError("the boxes of a Debye sweep share nx, ny and the relaxation rate")
+    for c in cases_:
+        f = c["flags"].reshape(c["shape"][2], ny, nx)
+        if not (np.all(f[0] == DIRICHLET) and np.all(f[-1] == DIRICHLET)):
+            raise ValueError("each box of a Debye sweep must be closed by Dirichlet planes in z")
+    flags = np.concatenate([c["flags"] for c in cases_])
+    phi = np.concatenate([c["dirichlet"] for c in cases_])
+    kz = np.concatenate([np.full(c["shape"][2], c["kappa_sq"]) for c in cases_])
+    nz = int(sum(c["shape"][2] for c in cases_))
+    return dict(lattice=D3Q7, shape=(nx, ny, nz), omega=omega, equation=1, kappa_sq=cases_[0]["kappa_sq"], flags=flags,
+                dirichlet=phi, faces=("wall",) * 6, slice_kappa_sq=kz.tolist(),
+                z0=np.cumsum([0] + [c["shape"][2] for c in cases_])[:-1].tolist())
 
 
 def box_kwargs(case: Dict) -> Dict:

@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(128) k_box_bnd(BoxParams P, const int32_t* lis
         f[q]            = S::load(A[src[q * n + i]]);
         if(corr_src) f[q] += static_cast<C>(corr_src[q * n + i]);
       });
-      const int z = P.slice_omega ? static_cast<int>(cell / (static_cast<int64_t>(P.nx) * P.ny)) : 0;
+      const int z = (P.slice_omega || P.slice_src) ? static_cast<int>(cell / (static_cast<int64_t>(P.nx) * P.ny)) : 0;
       collide<LAT, EQ, C>(P, z, f, MOM ? mom : nullptr);
     }
     if(corr_dst)
@@ -1126,6 +1126,8 @@ void box_destroy(BoxState* b) {
   cudaFree(b->dirichlet);
   cudaFree(b->slice_omega);
   cudaFree(b->slice_omega_f);
+  cudaFree(b->slice_src);
+  cudaFree(b->slice_src_f);
   cudaFree(b->mom);
   cudaFree(b->partials);
   cudaFree(b->out);
@@ -1705,6 +1707,40 @@ int lbm_gpu_box_set_slice_omega(lbm_gpu_ctx* ctx, const double* omega, int32_t n
   drop_graphs(b);
   b->p.slice_omega   = b->slice_omega;
   b->p.slice_omega_f = b->slice_omega_f;
+  return LBM_OK;
+}
+
+int lbm_gpu_box_set_slice_kappa(lbm_gpu_ctx* ctx, const double* kappa_sq, int32_t n) {
+  BoxState* b = lbm_internal_box(ctx);
+  if(!b) return LBM_ERR_INVALID;
+  if(b->desc.equation != LBM_POISSON) return LBM_ERR_UNSUPPORTED;
+  cudaStream_t s = lbm_internal_stream(ctx);
+  if(cudaStreamSynchronize(s) != cudaSuccess) return LBM_ERR_CUDA;
+  if(!kappa_sq) {
+    drop_graphs(b);  // the graphs hold the old launch parameters
+    b->p.slice_src   = nullptr;
+    b->p.slice_src_f = nullptr;
+    return LBM_OK;
+  }
+  if(n != b->p.nz) return LBM_ERR_INVALID;
+  // the same products the single-coefficient box forms (pb_diffusivity * kappa_sq)
+  std::vector<double> src(n);
+  std::vector<float>  srcf(n);
+  for(int z = 0; z < n; ++z) {
+    if(!(kappa_sq[z] >= 0.0 && std::isfinite(kappa_sq[z]))) return LBM_ERR_INVALID;
+    src[z]  = b->p.pb_diffusivity * kappa_sq[z];
+    srcf[z] = static_cast<float>(src[z]);
+  }
+  if(!b->slice_src) {
+    if(cudaMalloc(&b->slice_src, sizeof(double) * n) != cudaSuccess) return LBM_ERR_NOMEM;
+    if(cudaMalloc(&b->slice_src_f, sizeof(float) * n) != cudaSuccess) return LBM_ERR_NOMEM;
+  }
+  if(cudaMemcpy(b->slice_src, src.data(), sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+     cudaMemcpy(b->slice_src_f, srcf.data(), sizeof(float) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return LBM_ERR_CUDA;
+  drop_graphs(b);
+  b->p.slice_src   = b->slice_src;
+  b->p.slice_src_f = b->slice_src_f;
   return LBM_OK;
 }
 

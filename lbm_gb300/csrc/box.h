@@ -47,6 +47,10 @@ struct BoxParams {
   // per-z-slice relaxation rates (nz values each) or nullptr: one rate
   const double* slice_omega;
   const float*  slice_omega_f;
+  // per-z-slice Poisson-Boltzmann source coefficients alpha (1/2 - tau)
+  // kappa^2 (nz values each) or nullptr: pb_diffusivity * kappa_sq
+  const double* slice_src;
+  const float*  slice_src_f;
   const uint8_t* flags;     // ncells
   const double*  dirichlet; // ncells Poisson Dirichlet values or nullptr
   void*   pop;              // Q planes of nalloc values of the storage type
@@ -69,6 +73,8 @@ struct BoxState {
   double*      dirichlet = nullptr;
   double*      slice_omega   = nullptr;  // per-z-slice relaxation rates (lbm_gpu_box_set_slice_omega)
   float*       slice_omega_f = nullptr;
+  double*      slice_src     = nullptr;  // per-z-slice Poisson sources (lbm_gpu_box_set_slice_kappa)
+  float*       slice_src_f   = nullptr;
   void*        mom   = nullptr;
   double*      partials = nullptr;     // residual partials (one per step block and variable)
   double*      partials_mm = nullptr;  // mass / momentum partials

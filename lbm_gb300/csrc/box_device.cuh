@@ -158,7 +158,8 @@ __device__ __forceinline__ int64_t ghost_index(const BoxParams& P, int q, int y,
 // The collision of one cell of z-slice z.  FP64 arithmetic (FP64 storage)
 // works on the scaled deviation v; FP32 arithmetic (the other storages) on
 // the state shifted to the free stream (collide_ns_shifted, U = P.shift_u).
-// The relaxation rate is the slice's where the box has one per slice.
+// The relaxation rate (Navier-Stokes) or the source coefficient (Poisson) is
+// the slice's where the box has one per slice.
 template <int LAT, int EQ, class C>
 __device__ __forceinline__ void collide(const BoxParams& P, int z, C* v, C* mom_out) {
   if constexpr(EQ == LBM_NAVIER_STOKES) {
@@ -176,8 +177,8 @@ __device__ __forceinline__ void collide(const BoxParams& P, int z, C* v, C* mom_
       else collide_ns<LAT, C, false>(om, false, F, v, mom_out);
     }
   } else {
-    collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f), v,
-                            mom_out);
+    const C src = P.slice_src ? prm<C>(P.slice_src[z], P.slice_src_f[z]) : prm<C>(P.pb_diffusivity * P.kappa_sq, P.pb_src_f);
+    collide_poisson<LAT, C>(prm<C>(P.omega, P.omega_f), P.pb_nonlinear != 0, src, v, mom_out);
   }
 }
 

@@ -296,6 +296,17 @@ class BoxSolver:
         om = np.ascontiguousarray(omegas, dtype=np.float64)
         check(self._lib.lbm_gpu_box_set_slice_omega(self.ctx, _ptr(om), int(om.size)), self.ctx, "box_set_slice_omega")
 
+    def set_slice_kappa(self, kappa_sq: Optional[Sequence[float]]):
+        """One kappa^2 per z-slice (Poisson-Boltzmann boxes): boxes stacked
+        along z, each closed by Dirichlet planes, become a sweep over Debye
+        length in one launch per step; None restores the box's single
+        kappa^2."""
+        if kappa_sq is None:
+            check(self._lib.lbm_gpu_box_set_slice_kappa(self.ctx, None, 0), self.ctx, "box_set_slice_kappa")
+            return
+        k = np.ascontiguousarray(kappa_sq, dtype=np.float64)
+        check(self._lib.lbm_gpu_box_set_slice_kappa(self.ctx, _ptr(k), int(k.size)), self.ctx, "box_set_slice_kappa")
+
     def threads_per_block(self) -> int:
         t = C.c_int32()
         check(self._lib.lbm_gpu_box_autotune(self.ctx, C.byref(t)), self.ctx, "autotune")

@@ -8,7 +8,9 @@
   after 20,000 steps, which the CPU test of the two oracle forms bounds.
 * Config 4, D3Q7 Poisson-Boltzmann: in its linear (Debye-Hueckel) limit in a
   slab the potential matches sinh(kappa (L - x)) / sinh(kappa L); the
-  nonlinear sinh source matches the oracle on a seeded sphere case.
+  nonlinear sinh source matches the oracle on a seeded sphere case; a
+  Debye-length sweep of such boxes stacked along z steps each box as a box
+  of its own.
 """
 import numpy as np
 import pytest
@@ -16,6 +18,7 @@ import pytest
 import oracle
 from helpers import rel_l2
 from lbm_gb300 import cases
+from lbm_gb300._lib import LBMError
 from lbm_gb300.solver import BoxSolver
 
 pytestmark = pytest.mark.gpu
@@ -85,6 +88,45 @@ def test_config4_nonlinear_pb_spheres_match_oracle():
     f32.initial_condition()
     f32.step(200)
     assert rel_l2(f32.populations(), o.populations()) <= 1e-5
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_debye_sweep_boxes_step_as_boxes_of_their_own(storage):
+    """A Debye-length sweep: three charged-sphere boxes (different Debye
+    lengths and sphere sets, each closed by Dirichlet planes) stacked along z
+    in one D3Q7 box, each box's slices at its own kappa^2
+    (lbm_gpu_box_set_slice_kappa), step bit for bit as three boxes of their
+    own, nonlinear sinh source included."""
+    units = [cases.pb_spheres(n=24, seed=s, count=2) for s in (3, 5, 9)]
+    assert len({u["kappa_sq"] for u in units}) == 3
+    st = cases.stacked_debye(units)
+    g = BoxSolver(st["lattice"], st["shape"], st["omega"], storage, pb_nonlinear=True, **cases.box_kwargs(st))
+    g.set_slice_kappa(st["slice_kappa_sq"])
+    g.initial_condition()
+    g.step(61)
+    f = g.populations()
+    n3 = 24 ** 3
+    for k, u in enumerate(units):
+        s1 = BoxSolver(u["lattice"], u["shape"], u["omega"], storage, pb_nonlinear=True, **cases.box_kwargs(u))
+        s1.initial_condition()
+        s1.step(61)
+        assert np.array_equal(f[:, k * n3:(k + 1) * n3], s1.populations()), k
+        s1.close()
+    # the box's single kappa^2 again: the middle box at the first box's kappa^2
+    g.set_slice_kappa(None)
+    g.initial_condition()
+    g.step(8)
+    s1 = BoxSolver(units[1]["lattice"], units[1]["shape"], units[1]["omega"], storage, pb_nonlinear=True,
+                   **dict(cases.box_kwargs(units[1]), kappa_sq=units[0]["kappa_sq"]))
+    s1.initial_condition()
+    s1.step(8)
+    assert np.array_equal(g.populations()[:, n3:2 * n3], s1.populations())
+    s1.close()
+    with pytest.raises(LBMError):
+        g.set_slice_kappa([0.01, 0.02])  # not one value per slice
+    with pytest.raises(LBMError):
+        g.set_slice_kappa([-1.0] * st["shape"][2])  # negative kappa^2
+    g.close()
 
 
 def test_config2_sphere_sample_fp64_matches_oracle_over_201_steps():
