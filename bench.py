@@ -694,6 +694,27 @@ def profile_case(args):
         torch.cuda.synchronize()
         rng.range_pop()
         return {"profile_case": "cavities", "domains": 256, "cells": b.ncells, "tuning": b.tuning()}
+    if args.profile_case == "table":
+        # the reference-table engine (the reference's phase sequence, FP64,
+        # int32 pull table) on the own lid-driven cavity config at level 10:
+        # 1024 x 1024 cells, state and tables larger than L2
+        from lbm_gb300.solver import LBMSolver
+
+        cfg = json.load(open(os.path.join(ROOT, "tests", "golden", "cases", "cavity_small.json")))
+        cfg.update({"partitionLevel": 10, "uniformLevel": 10, "maxRfnmtLvl": 10})
+        s = LBMSolver.from_config(cfg)
+        g = s.gpu
+        g.initial_condition()
+        g.step(16)
+        t0 = time.perf_counter()
+        g.step(400)
+        wall = time.perf_counter() - t0
+        rng.range_push("profile")
+        g.step(8)
+        rng.range_pop()
+        n = s.grid.ncells
+        return {"profile_case": "table", "cells": n, "host_timed_mlups_400_steps": n * 400 / wall / 1e6,
+                "ms_per_step": wall / 400 * 1e3}
     if args.profile_case == "poisson":
         from lbm_gb300 import cases
         from lbm_gb300.solver import BoxSolver
@@ -746,7 +767,7 @@ def main():
     ap.add_argument("--cavity-steps", type=int, default=2000, help="step bound of the cavities' convergence run")
     ap.add_argument("--cavity-check", type=int, default=1, help="cavities: also run a subset to convergence in FP64 and FP32 (1) or not (0)")
     ap.add_argument("--acc-full-steps", type=int, default=0, help="accuracy: only the full 512x256x256 box, to this many steps")
-    ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL) + ["cavities", "poisson", "unet"],
+    ap.add_argument("--profile-case", default=None, choices=list(B_PER_CELL) + ["cavities", "poisson", "unet", "table"],
                     help="a small case for ncu captures, its measured launches inside the NVTX range 'profile': 4 steps of "
                          "a 256x128x128 version of the sphere workload in this storage; or 4 steps of 256 of the cavities; "
                          "or 4 steps of the D3Q7 Poisson-Boltzmann 256^3 case (FP32); or one training step of the U-Net "

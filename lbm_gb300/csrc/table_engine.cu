@@ -42,13 +42,41 @@ inline unsigned blocks(int64_t n) { return static_cast<unsigned>((n + TPB - 1) /
 
 __device__ __forceinline__ int64_t gid() { return static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; }
 
+// x / c for the equilibrium's constant divisors c = c_s^2, 2 c_s^4, 2 c_s^2,
+// correctly rounded, from y = RN(1/c): q0 = x y, r = x - c q0 (one fused
+// multiply-add, exact), q = RN(q0 + r y).  For these three constants
+// |y c - 1| = 2^-54, so q0 is within half an ulp of x / c and thus one of the
+// two doubles around it, and Markstein's theorem (P. Markstein, IBM J. Res.
+// Dev. 34(1), 1990: y within half an ulp of 1/c, q0 within one ulp of x / c
+// => RN(q0 + r y) = RN(x / c)) makes q the IEEE quotient.  A full FP64
+// division costs several times the three FP64 operations on this part's
+// narrow FP64 pipe, which bounds the collision kernel.  Zeros, infinities
+// and NaNs (exponent field 0 or all ones, tested on the integer side) pass
+// through as x y; the state never reaches subnormal magnitudes.  Checked
+// against IEEE division on 60 million doubles (tests/test_const_div.py) and,
+// through the engine, bit for bit against the reference's solver.
+struct ConstDiv {
+  double c, y;
+};
+constexpr ConstDiv DIV_CS2{CSSQ, 1.0 / CSSQ};
+constexpr ConstDiv DIV_2CS4{2.0 * CSSQ * CSSQ, 1.0 / (2.0 * CSSQ * CSSQ)};
+constexpr ConstDiv DIV_2CS2{2.0 * CSSQ, 1.0 / (2.0 * CSSQ)};
+
+__device__ __forceinline__ double div_const(double x, ConstDiv d) {
+  const double q = x * d.y;
+  const int    e = (__double2hiint(q) >> 20) & 0x7ff;
+  if(e == 0 || e == 0x7ff) return q;
+  const double r = __fma_rn(-q, d.c, x);
+  return __fma_rn(r, d.y, q);
+}
+
 // eq::defaultEq(w, rho, cu, vsq), src/lbm/equilibrium_func.h:52-54
 __device__ __forceinline__ double eq_default(double w, double rho, double cu, double vsq) {
-  return w * rho * (1.0 + cu / CSSQ + cu * cu / (2.0 * CSSQ * CSSQ) - vsq / (2.0 * CSSQ));
+  return w * rho * (1.0 + div_const(cu, DIV_CS2) + div_const(cu * cu, DIV_2CS4) - div_const(vsq, DIV_2CS2));
 }
 // eq::symmEq, src/lbm/equilibrium_func.h:109-111
 __device__ __forceinline__ double eq_symm(double w, double rho, double cu, double vsq) {
-  return w * rho * (1.0 + cu * cu / (2.0 * CSSQ * CSSQ) - vsq / (2.0 * CSSQ));
+  return w * rho * (1.0 + div_const(cu * cu, DIV_2CS4) - div_const(vsq, DIV_2CS2));
 }
 
 template <int LAT>
