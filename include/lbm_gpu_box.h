@@ -45,7 +45,14 @@ typedef enum lbm_storage {
   LBM_STORE_F64     = 0, /* FP64 storage, FP64 arithmetic (the plain method) */
   LBM_STORE_F32     = 1, /* FP32 storage, FP32 arithmetic */
   LBM_STORE_F16_DEV = 2, /* FP16 storage, FP32 arithmetic */
-  LBM_STORE_BF16_DEV = 3 /* BF16 storage, FP32 arithmetic */
+  LBM_STORE_BF16_DEV = 3, /* BF16 storage, FP32 arithmetic */
+  /* A 16-bit float of 1 sign, 3 exponent and 12 mantissa bits (13
+   * significant bits) holding s_i / 1024: normal from 2^-6 to 2 - 2^-12,
+   * evenly spaced (2^-18) below, rounded to nearest even, saturating at the
+   * largest magnitude (no infinities or NaNs: a diverging state saturates).
+   * Two more significant bits than FP16 over the range the shifted state
+   * occupies, at the same bytes; FP32 arithmetic.  Navier-Stokes only. */
+  LBM_STORE_E3M12_DEV = 4
 } lbm_storage;
 
 /* treatment of a face of the box */

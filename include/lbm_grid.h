@@ -4,7 +4,9 @@
  * subtracted objects), the uniform Cartesian grid that the SFCMM/LBM
  * reference's grid generator and CartesianGrid produce when
  * partitionLevel == uniformLevel == maxRfnmtLvl (every reference LBM case),
- * and the tables its LBM solver reads:
+ * and the tables its LBM solver reads (for multi-level grids the tree calls
+ * at the end of this header build the cells, lbm_grid_tree_grid hands them
+ * to the same table calls):
  *
  *   entry point                  reference step it replaces
  *   lbm_grid_create              GridGenerator::init / createPartitioningGrid, deleteOutsideCells,
@@ -159,6 +161,17 @@ int lbm_grid_tree_neighbors(const lbm_grid_tree* t, int64_t* out);
  * a header of the axis names and the columns, then one line per cell with
  * the centre at 15 significant digits and the listed columns */
 int lbm_grid_tree_write_points(const lbm_grid_tree* t, const char* path, const int32_t* columns, int32_t ncolumns);
+/* The tree's cells as the LBM solver's grid loads them
+ * (CartesianGrid::loadGridInplace, src/cartesiangrid.h:264-320): every cell
+ * of every level, in the tree's order, with its same-level neighbours; the
+ * boundary property as determineBoundaryCells sets it (:509-544: a cell
+ * whose parent is not a boundary cell is not one); surfaces cut with the
+ * length of each cell's level.  The result takes the calls after
+ * lbm_grid_create (lbm_grid_add_surface, lbm_grid_connect_periodic,
+ * lbm_grid_neighbors, lbm_grid_destroy); alignment is the tree's own.  The
+ * reference's solver steps every level of such a grid as a lattice of its
+ * own (src/lbm/solver.cpp:525). */
+int lbm_grid_tree_grid(const lbm_grid_tree* t, lbm_grid** out);
 void lbm_grid_tree_destroy(lbm_grid_tree* t);
 
 #ifdef __cplusplus

@@ -300,6 +300,17 @@ struct Pair<LBM_STORE_BF16_DEV> {
     *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
   }
 };
+template <>
+struct Pair<LBM_STORE_E3M12_DEV> {
+  static __device__ __forceinline__ void load(const uint16_t* p, float& a, float& b) {
+    const uint32_t w = *reinterpret_cast<const uint32_t*>(p);
+    a                = e3m12_decode(static_cast<uint16_t>(w & 0xffffu));
+    b                = e3m12_decode(static_cast<uint16_t>(w >> 16));
+  }
+  static __device__ __forceinline__ void store(uint16_t* p, float a, float b) {
+    *reinterpret_cast<uint32_t*>(p) = static_cast<uint32_t>(e3m12_encode(a)) | (static_cast<uint32_t>(e3m12_encode(b)) << 16);
+  }
+};
 
 // k_box_pair: the plain (MOM = 0) bulk step with two x-adjacent cells per
 // thread (nx even, so a pair never straddles a row and starts on an even
@@ -876,10 +887,12 @@ cudaError_t launch_load(BoxState* b, const double* in, cudaStream_t s) {
       case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return FN<LBM_D2Q9, 0, LBM_STORE_F32>(__VA_ARGS__);         \
       case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return FN<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(__VA_ARGS__); \
       case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return FN<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(__VA_ARGS__); \
+      case LBM_D2Q9 * 100 + 0 + LBM_STORE_E3M12_DEV: return FN<LBM_D2Q9, 0, LBM_STORE_E3M12_DEV>(__VA_ARGS__); \
       case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return FN<LBM_D3Q19, 0, LBM_STORE_F64>(__VA_ARGS__);       \
       case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return FN<LBM_D3Q19, 0, LBM_STORE_F32>(__VA_ARGS__);       \
       case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return FN<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(__VA_ARGS__); \
       case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return FN<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(__VA_ARGS__); \
+      case LBM_D3Q19 * 100 + 0 + LBM_STORE_E3M12_DEV: return FN<LBM_D3Q19, 0, LBM_STORE_E3M12_DEV>(__VA_ARGS__); \
       case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return FN<LBM_D3Q7, 1, LBM_STORE_F64>(__VA_ARGS__);        \
       case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return FN<LBM_D3Q7, 1, LBM_STORE_F32>(__VA_ARGS__);        \
       default: return cudaErrorInvalidValue;                                                               \
@@ -1209,7 +1222,8 @@ int lbm_gpu_box_storage_bytes(int32_t storage) {
     case LBM_STORE_F64: return 8;
     case LBM_STORE_F32: return 4;
     case LBM_STORE_F16_DEV:
-    case LBM_STORE_BF16_DEV: return 2;
+    case LBM_STORE_BF16_DEV:
+    case LBM_STORE_E3M12_DEV: return 2;
     default: return 0;
   }
 }
@@ -1218,7 +1232,7 @@ int lbm_gpu_create_box(const lbm_box_desc* desc, const uint8_t* flags, const dou
   if(!desc || !out) return LBM_ERR_INVALID;
   *out = nullptr;
   const int lat = desc->lattice, eq = desc->equation, st = desc->storage;
-  const bool ok = ((lat == LBM_D2Q9 || lat == LBM_D3Q19) && eq == LBM_NAVIER_STOKES && st >= 0 && st <= 3) ||
+  const bool ok = ((lat == LBM_D2Q9 || lat == LBM_D3Q19) && eq == LBM_NAVIER_STOKES && st >= 0 && st <= LBM_STORE_E3M12_DEV) ||
                   (lat == LBM_D3Q7 && eq == LBM_POISSON && (st == LBM_STORE_F64 || st == LBM_STORE_F32));
   if(!ok) return LBM_ERR_UNSUPPORTED;
   const int D = lat == LBM_D2Q9 ? 2 : 3;

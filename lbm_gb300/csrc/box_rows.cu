@@ -496,10 +496,12 @@ cudaError_t box_rows_bulk(BoxState* b, bool odd, int mom, cudaStream_t s, int64_
     case LBM_D2Q9 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F32>(b, odd, mom, s, nbulk);
     case LBM_D2Q9 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, nbulk);
     case LBM_D2Q9 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D2Q9 * 100 + 0 + LBM_STORE_E3M12_DEV: return launch_rows<LBM_D2Q9, 0, LBM_STORE_E3M12_DEV>(b, odd, mom, s, nbulk);
     case LBM_D3Q19 * 100 + 0 + LBM_STORE_F64: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F64>(b, odd, mom, s, nbulk);
     case LBM_D3Q19 * 100 + 0 + LBM_STORE_F32: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F32>(b, odd, mom, s, nbulk);
     case LBM_D3Q19 * 100 + 0 + LBM_STORE_F16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_F16_DEV>(b, odd, mom, s, nbulk);
     case LBM_D3Q19 * 100 + 0 + LBM_STORE_BF16_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_BF16_DEV>(b, odd, mom, s, nbulk);
+    case LBM_D3Q19 * 100 + 0 + LBM_STORE_E3M12_DEV: return launch_rows<LBM_D3Q19, 0, LBM_STORE_E3M12_DEV>(b, odd, mom, s, nbulk);
     case LBM_D3Q7 * 100 + 10 + LBM_STORE_F64: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F64>(b, odd, mom, s, nbulk);
     case LBM_D3Q7 * 100 + 10 + LBM_STORE_F32: return launch_rows<LBM_D3Q7, 1, LBM_STORE_F32>(b, odd, mom, s, nbulk);
     default: return cudaErrorInvalidValue;

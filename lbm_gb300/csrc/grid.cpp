@@ -414,8 +414,10 @@ int lbm_grid_add_surface(lbm_grid* g, int32_t obj, int32_t dir_begin, int32_t di
   // the pairs of this surface: a boundary cell without a main neighbour in
   // the direction, cut by the object, and not taken by an earlier surface
   // (within one call a pair cannot repeat, so counting needs no marks)
+  // the cut test with the length of the cell's level
   auto member = [&](int64_t c, int dir) {
-    return g->nbr[c * M + dir] == -1 && !(g->assigned[c] & (1u << dir)) && obj_cut(g->objs[obj], &g->centers[c * D], g->cell_length, D);
+    const double len = g->cell_len.empty() ? g->cell_length : g->cell_len[c];
+    return g->nbr[c * M + dir] == -1 && !(g->assigned[c] & (1u << dir)) && obj_cut(g->objs[obj], &g->centers[c * D], len, D);
   };
   int64_t count = 0;
   for(int dir = dir_begin; dir < dir_end; ++dir)

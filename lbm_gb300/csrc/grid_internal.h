@@ -24,6 +24,7 @@ struct lbm_grid {
   std::vector<uint8_t>       bndry;      // boundary property
   std::vector<int64_t>       bcells;     // the boundary cells, ascending
   std::vector<uint8_t>       assigned;   // per cell: bit d set when (cell, d) belongs to a surface
+  std::vector<double>        cell_len;   // per-cell level length (multi-level grids); empty: cell_length for all
 
   lbm_grid_geom::GeomSet geom() const {
     lbm_grid_geom::GeomSet s;
@@ -45,4 +46,7 @@ void link_cells(lbm_grid& g);
 void list_boundary_cells(lbm_grid& g);
 // hilbert::index (include/common/math/hilbert.h:16-48) of a point of the unit cube
 uint64_t curve_index(const double* x, int D, int level);
+// analytic geometry tests of the grid's objects
+bool geom_cut(const lbm_grid& g, const double* c, double len);
+bool geom_inside(const lbm_grid& g, const double* x);
 }  // namespace lbm_grid_impl

@@ -44,7 +44,10 @@
 
 struct lbm_grid_tree {
   int                  D = 0, nc = 0, nn = 0;
-  int                  partition_level = 0, highest_level = 0;
+  int                  partition_level = 0, highest_level = 0, max_level = 0;
+  lbm_grid             geom;          // geometry, bounding box and root length (no cells)
+  std::vector<double>  len;           // the generator's cell length per level (maxRfnmtLvl's stretched by alignment)
+  double               max_len_solver = 0;  // maxRfnmtLvl's length as the solver's grid takes it over
   int64_t              n = 0;
   std::vector<double>  centers;   // n x D
   std::vector<int8_t>  level;     // n
@@ -412,6 +415,20 @@ int lbm_grid_tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_
   t->nn              = nn;
   t->partition_level = partition_level;
   t->highest_level   = highest;
+  t->max_level       = max_level;
+  t->len             = g.len;
+  // the solver's grid takes maxRfnmtLvl's length over as the ratio of the
+  // generator's stretched length to its own (transformMaxLvl,
+  // src/cartesiangrid.h:274)
+  {
+    double solver_len = base.len0;
+    for(int l = 1; l <= max_level; ++l) solver_len = 0.5 * solver_len;
+    t->max_len_solver = solver_len * (g.len[max_level] / solver_len);
+  }
+  base.cv[0].clear();
+  base.cv[1].clear();
+  base.cv[2].clear();
+  t->geom = std::move(base);
   // flatten: the levels lie one after the other from slot 0
   std::vector<int64_t> off(levels.size() + 1, 0);
   for(size_t i = 0; i < levels.size(); ++i) off[i + 1] = off[i] + levels[i].n;
@@ -511,6 +528,56 @@ int lbm_grid_tree_write_points(const lbm_grid_tree* t, const char* path, const i
   }
   ok = (std::fclose(f) == 0) && ok;
   return ok ? LBM_OK : LBM_ERR_INVALID;
+}
+
+int lbm_grid_tree_grid(const lbm_grid_tree* t, lbm_grid** out) {
+  if(!t || !out) return LBM_ERR_INVALID;
+  *out = nullptr;
+  if(t->n >= (int64_t(1) << 31)) return LBM_ERR_INVALID;
+  lbm_grid* g = new(std::nothrow) lbm_grid();
+  if(!g) return LBM_ERR_NOMEM;
+  const int D = t->D, nn = t->nn;
+  try {
+    g->D     = D;
+    g->level = t->max_level;
+    g->objs  = t->geom.objs;
+    g->body  = t->geom.body;
+    g->nbody = t->geom.nbody;
+    for(int d = 0; d < 3; ++d) {
+      g->bmin[d] = t->geom.bmin[d];
+      g->bmax[d] = t->geom.bmax[d];
+      g->cog[d]  = t->geom.cog[d];
+    }
+    g->len0        = t->geom.len0;
+    g->cell_length = t->max_len_solver;
+    g->cut_length  = t->len[t->max_level];
+    g->n           = t->n;
+    g->centers     = t->centers;
+    g->nbr         = t->nghbr;
+    // the solver's length of each cell's level: the generator's, and
+    // maxRfnmtLvl's as the solver takes it over
+    g->cell_len.resize(t->n);
+    for(int64_t c = 0; c < t->n; ++c)
+      g->cell_len[c] = t->level[c] == t->max_level ? t->max_len_solver : t->len[t->level[c]];
+    // determineBoundaryCells (src/cartesiangrid.h:509-544) in cell order: a
+    // cell without a parent, or whose parent is a boundary cell, is one when
+    // cut and missing a main neighbour; any other cell is not
+    g->bndry.assign(t->n, 0);
+    for(int64_t c = 0; c < t->n; ++c) {
+      const int64_t p = t->parent[c];
+      if(p >= 0 && !(p < c && g->bndry[p])) continue;
+      if(!geom_cut(*g, &g->centers[c * D], g->cell_len[c])) continue;
+      int present = 0;
+      for(int dir = 0; dir < nn; ++dir) present += g->nbr[c * nn + dir] >= 0 ? 1 : 0;
+      g->bndry[c] = present < nn ? 1 : 0;
+    }
+  } catch(const std::bad_alloc&) {
+    delete g;
+    return LBM_ERR_NOMEM;
+  }
+  list_boundary_cells(*g);
+  *out = g;
+  return LBM_OK;
 }
 
 void lbm_grid_tree_destroy(lbm_grid_tree* t) { delete t; }

@@ -49,6 +49,40 @@ struct Store<LBM_STORE_BF16_DEV> {
   static __device__ __forceinline__ C load(T v) { return __bfloat162float(v); }
   static __device__ __forceinline__ T store(C v) { return __float2bfloat16_rn(v); }
 };
+// 1 sign, 3 exponent, 12 mantissa bits of t = s / 1024 (LBM_STORE_E3M12_DEV):
+// code = E * 4096 + m, value 2^(E-7) (1 + m / 4096) for E >= 1 and
+// 2^-6 m / 4096 for E = 0, saturating at code 0x7fff.  Encoding, for
+// |s| >= 16 (t >= 2^-6, E >= 1): the FP32 bits of |s| rounded to 12 mantissa
+// bits (round to nearest even on the 11 dropped bits, the carry moving into
+// the exponent) and rebased from FP32's exponent bias and the 2^-10 scale to
+// the code's (130 = 127 + 10 - 7); below: round(|s| 2^8) as an integer (the
+// evenly spaced range, 2^-18 in t; 4096 rounds into the first normal code).
+// Decoding: the code's 15 bits placed as FP32 bits (exponent field E,
+// mantissa m << 11) are 2^-130 times the value, E = 0 included (an FP32
+// subnormal then), so two exact power-of-two products restore it.
+__device__ __forceinline__ uint16_t e3m12_encode(float s) {
+  const uint32_t u = __float_as_uint(s);
+  const uint32_t a = u & 0x7fffffffu;
+  uint32_t       code;
+  if(a >= 0x41800000u) {  // |s| >= 16
+    const uint32_t r = a + 0x3ffu + ((a >> 11) & 1u);
+    code             = min((r >> 11) - (130u << 12), 0x7fffu);
+  } else {
+    code = __float2uint_rn(__uint_as_float(a) * 256.0f);
+  }
+  return static_cast<uint16_t>(code | ((u >> 16) & 0x8000u));
+}
+__device__ __forceinline__ float e3m12_decode(uint16_t c) {
+  const uint32_t bits = ((static_cast<uint32_t>(c) & 0x7fffu) << 11) | ((static_cast<uint32_t>(c) & 0x8000u) << 16);
+  return __uint_as_float(bits) * 0x1p127f * 8.0f;
+}
+template <>
+struct Store<LBM_STORE_E3M12_DEV> {
+  using T = uint16_t;
+  using C = float;
+  static __device__ __forceinline__ C load(T v) { return e3m12_decode(v); }
+  static __device__ __forceinline__ T store(C v) { return e3m12_encode(v); }
+};
 
 // state value <-> population f of direction q
 template <int LAT, int EQ>

@@ -5,8 +5,10 @@ generator (``src/gridgenerator/``) makes the cells, and ``CartesianGrid::
 loadGridInplace`` (src/cartesiangrid.h:264-320) derives the boundary cells,
 the named boundary surfaces, the periodic wiring and the diagonal neighbours.
 :func:`grid_tables` does both for the uniform grids every reference LBM case
-uses (``partitionLevel == uniformLevel == maxRfnmtLvl``) and returns the
-:class:`~lbm_gb300.refconfig.GridTables` the solvers consume.  The per-cell
+uses (``partitionLevel == uniformLevel == maxRfnmtLvl``), and for multi-level
+grids, whose every level the reference's solver steps as a lattice of its
+own, and returns the :class:`~lbm_gb300.refconfig.GridTables` the solvers
+consume.  The per-cell
 work runs in the native library (include/lbm_grid.h); this module walks the
 config in the reference's order:
 
@@ -80,6 +82,7 @@ _SIGS = {
     "lbm_grid_tree_children": (C.c_int, [C.c_void_p, C.c_void_p]),
     "lbm_grid_tree_neighbors": (C.c_int, [C.c_void_p, C.c_void_p]),
     "lbm_grid_tree_write_points": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p, C.c_int32]),
+    "lbm_grid_tree_grid": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "lbm_grid_tree_destroy": (None, [C.c_void_p]),
 }
 
@@ -144,12 +147,9 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
         raise ConfigError(f"dim must be 1, 2 or 3, got {ndim}")
     levels = {k: int(config[k]) for k in ("partitionLevel", "uniformLevel", "maxRfnmtLvl") if k in config}
     level = levels.get("uniformLevel", levels.get("partitionLevel"))
-    if level is None or len(set(levels.values())) != 1:
-        # the reference's solver would step every level of a multi-level
-        # array as a lattice of its own (src/lbm/solver.cpp:525); the
-        # generator's tree for such a config is grid_tree's
-        raise ConfigError("the LBM tables are built for uniform grids: partitionLevel, uniformLevel and maxRfnmtLvl must be "
-                          "equal (grid_tree builds the generator's multi-level tree)")
+    if level is None:
+        raise ConfigError('"partitionLevel" and "uniformLevel" are required')
+    multilevel = len(set(levels.values())) != 1
     geometry = config.get("geometry", {})
     descs, names = geometry_objects(geometry, ndim)
     bbox = None
@@ -159,13 +159,34 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
     lib = _grid_lib()
     h = C.c_void_p()
     pb = C.cast(bbox, C.c_void_p) if bbox else None
-    if device is None:
-        rc = lib.lbm_grid_create(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, C.byref(h))
+    if multilevel:
+        # every level of the generator's array, as the reference's solver
+        # loads and steps it (src/lbm/solver.cpp:525: each level a lattice
+        # of its own); built on the host
+        p, u, level, cap = _tree_levels(config)
+        for gname, entries in config.get("solver", {}).get("boundary", {}).items():
+            for e in entries.values():
+                if isinstance(e, dict) and e.get("type") == "periodic" and e.get("generateBndry", True):
+                    # its mapping steps one cell length of the mapped cell's
+                    # level; the engine maps with one length
+                    raise ConfigError(f'periodic boundary condition "{gname}" (generateBndry) on a multi-level grid is not '
+                                      "supported")
+        align = int(config.get("alignDir", 1)) if config.get("alignNodesWithSurface", False) else -1
+        t = C.c_void_p()
+        _lib.check(lib.lbm_grid_tree_create(ndim, p, u, level, cap, C.cast(descs, C.c_void_p), len(names), pb, align, C.byref(t)),
+                   what="lbm_grid_tree_create")
+        try:
+            _lib.check(lib.lbm_grid_tree_grid(t, C.byref(h)), what="lbm_grid_tree_grid")
+        finally:
+            lib.lbm_grid_tree_destroy(t)
     else:
-        rc = lib.lbm_grid_create_device(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, int(device), C.byref(h))
-    _lib.check(rc, what="lbm_grid_create")
+        if device is None:
+            rc = lib.lbm_grid_create(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, C.byref(h))
+        else:
+            rc = lib.lbm_grid_create_device(ndim, level, C.cast(descs, C.c_void_p), len(names), pb, int(device), C.byref(h))
+        _lib.check(rc, what="lbm_grid_create")
     try:
-        if config.get("alignNodesWithSurface", False):
+        if config.get("alignNodesWithSurface", False) and not multilevel:
             _lib.check(lib.lbm_grid_align(h, int(config.get("alignDir", 1))), what="lbm_grid_align")
         n = int(lib.lbm_grid_ncells(h))
         centers = np.empty((n, ndim), dtype=np.float64)

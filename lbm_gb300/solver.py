@@ -139,7 +139,7 @@ class TableSolver:
 
 
 FACE = {"wall": 0, "periodic": 1, "freeslip": 2, "open": 3}
-STORAGE = {"f64": 0, "f32": 1, "f16dev": 2, "bf16dev": 3}
+STORAGE = {"f64": 0, "f32": 1, "f16dev": 2, "bf16dev": 3, "e3m12dev": 4}
 STORAGE_BYTES = {0: 8, 1: 4, 2: 2, 3: 2}
 
 

@@ -19,7 +19,10 @@
  *          6 a 16-bit float of 1 sign, 4 exponent and 11 mantissa bits
  *            (Lehmann et al., Phys. Rev. E 106, 015308 (2022)) of s / S x 4:
  *            12 significant bits, normal range [2^-14, 2), saturating;
- *          8 16-bit fixed point of s: round(s / S x 2^15) / 2^15, saturating;
+ *          7 a 16-bit float of 1 sign, 3 exponent and 12 mantissa bits of
+            s / S x 4: 13 significant bits, normal range [2^-6, 2),
+            subnormal below, saturating;
+          8 16-bit fixed point of s: round(s / S x 2^15) / 2^15, saturating;
           9 block floating point of s: per cell, 16-bit integers times one
             power-of-two scale 2^(e - 15) with 2^e >= the cell's max |s|;
           10 the same with the scale of the slot's owner, as the AA pattern
@@ -129,6 +132,7 @@ static double store(double x, int q, uint32_t i, uint32_t t) {
       return copysign(floor(a / ulp + r) * ulp, x);
     }
     case 6: return round_fp(x / 4096.0 * 4.0, 12, -14, 2.0 - ldexp(1, -11)) / 4.0 * 4096.0;
+    case 7: return round_fp(x / 4096.0 * 4.0, 13, -6, 2.0 - ldexp(1, -12)) / 4.0 * 4096.0;
     case 8: {
       double v = nearbyint(x / 4096.0 * 32768.0);
       if(v > 32767) v = 32767;

@@ -27,6 +27,7 @@ VARIANTS = [
     (4, 0, "FP16 of the shifted state, FP64 arithmetic"),
     (14, 2, "FP16 of the shifted state with stochastic rounding, FP32 arithmetic"),
     (6, 2, "1-4-11 16-bit float of the shifted state, FP32 arithmetic"),
+    (7, 2, "1-3-12 16-bit float of the shifted state, FP32 arithmetic"),
     (8, 2, "16-bit fixed point of the shifted state, FP32 arithmetic"),
     (9, 2, "16-bit block floating point of the shifted state (one exponent per cell), FP32 arithmetic"),
     (10, 2, "the same with the slot owner's exponent as AA in-place streaming would hold it, FP32 arithmetic"),

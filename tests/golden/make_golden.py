@@ -65,6 +65,15 @@ CASES = [
     # inlet / outlet, bounce-back walls) at level 5 instead of 8
     ("sphere_ns_l5", ("ref", "test/sphere/sphere_ns.json", {"partitionLevel": 5, "uniformLevel": 5, "maxRfnmtLvl": 5}),
      [1, 60, 1000]),
+    # multi-level grids: the solver loads every level of the generator's array
+    # and steps each as a lattice of its own (src/lbm/solver.cpp:525)
+    ("poiseuille_p3u5", ("ref", "test/poiseuille/poiseuille.json", {"partitionLevel": 3, "uniformLevel": 5, "maxRfnmtLvl": 5}),
+     [20, 1000]),
+    ("cavity_p2u3m5", ("own", "cavity_small.json", {"partitionLevel": 2, "uniformLevel": 3, "maxRfnmtLvl": 5}), [100]),
+    ("cavity_obstacle_p2u3m6", ("own", "cavity_obstacle_small.json", {"partitionLevel": 2, "uniformLevel": 3, "maxRfnmtLvl": 6}),
+     [100]),
+    ("poisson2d_helmholtz_p2u3m5", ("own", "poisson2d_helmholtz_small.json",
+                                    {"partitionLevel": 2, "uniformLevel": 3, "maxRfnmtLvl": 5}), [100]),
 ]
 
 
@@ -168,7 +177,8 @@ def run_line(name, steps, tag, a, b):
 # the grid part of every case's config (grid generator keys, geometry and the
 # solver's boundary block): tests/golden/grid_configs.json, the input of the
 # grid-table tests (the reference's own test configs are not read at test time)
-GRID_KEYS = ("dim", "partitionLevel", "uniformLevel", "maxRfnmtLvl", "boundingBox", "alignNodesWithSurface", "alignDir", "geometry")
+GRID_KEYS = ("dim", "partitionLevel", "uniformLevel", "maxRfnmtLvl", "maxNoCells", "boundingBox", "alignNodesWithSurface", "alignDir",
+             "geometry")
 
 
 def write_grid_configs():

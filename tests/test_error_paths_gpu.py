@@ -93,3 +93,34 @@ def test_staged_kernel_wait_timeout_reports_timeout(storage, kernel):
         ref.initial_condition()
         ref.step(45)
         assert np.array_equal(g.populations(), ref.populations())
+
+
+# A channel with pressure boundaries and an obstacle on a multi-level grid
+# (partitioning level 2, uniform 3, boundary cells refined to 5): on the
+# refined levels some -x / +x boundary cells have no second cell inside.
+PRESSURE_MULTILEVEL = {
+    "dim": 2, "partitionLevel": 2, "uniformLevel": 3, "maxRfnmtLvl": 5, "maxNoCells": 100000,
+    "geometry": {"cube": {"type": "box", "body": "fluid", "A": [0.0, 0.0], "B": [4.0, 2.0]},
+                 "obstacle": {"type": "sphere", "body": "fluid", "subtract": True, "center": [1.3, 1.05], "radius": 0.35}},
+    "solver": {"type": "lbm", "relaxation": 0.8, "ma": 0.1, "maxSteps": 10,
+               "boundary": {"cube": {"-x": {"type": "pressure", "pressure": 1.0000008}, "+x": {"type": "pressure", "pressure": 1.0},
+                                     "-y": {"type": "wall", "model": "bounceback"}, "+y": {"type": "wall", "model": "bounceback"}},
+                            "obstacle": {"all": {"type": "wall", "model": "bounceback"}}}}}
+
+
+def test_multilevel_boundary_without_its_stencil_is_refused():
+    """Boundary conditions whose stencil leaves the grid on a multi-level
+    grid are refused when the table is uploaded (LBM_ERR_TABLE), before any
+    kernel runs.  The reference does not check this for the pressure
+    boundary: it reads the neighbour table at index -1 there
+    (src/lbm/bnd/bnd_pressure.h:73-78)."""
+    from lbm_gb300 import gridgen
+    from lbm_gb300.solver import LBMSolver
+
+    g = gridgen.grid_tables(PRESSURE_MULTILEVEL)
+    cells = g.surfaces["cube_-x"]["cells"]
+    inside = g.nghbr[cells, 1]
+    assert np.any((inside < 0) | (g.nghbr[np.maximum(inside, 0), 1] < 0)), "the case must miss an inside cell"
+    with pytest.raises(LBMError) as e:
+        LBMSolver.from_config(PRESSURE_MULTILEVEL)
+    assert e.value.code == -3
