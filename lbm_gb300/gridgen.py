@@ -176,6 +176,13 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
         _lib.check(lib.lbm_grid_tree_create(ndim, p, u, level, cap, C.cast(descs, C.c_void_p), len(names), pb, align, C.byref(t)),
                    what="lbm_grid_tree_create")
         try:
+            nt = int(lib.lbm_grid_tree_ncells(t))
+            pl, hl = C.c_int32(), C.c_int32()
+            _lib.check(lib.lbm_grid_tree_levels(t, C.byref(pl), C.byref(hl)), what="lbm_grid_tree_levels")
+            tree_level = np.empty(nt, dtype=np.int8)
+            tree_nchildren = np.empty(nt, dtype=np.int32)
+            _lib.check(lib.lbm_grid_tree_cells(t, None, tree_level.ctypes.data, None, None, tree_nchildren.ctypes.data, None),
+                       what="lbm_grid_tree_cells")
             _lib.check(lib.lbm_grid_tree_grid(t, C.byref(h)), what="lbm_grid_tree_grid")
         finally:
             lib.lbm_grid_tree_destroy(t)
@@ -252,8 +259,9 @@ def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
         _lib.check(lib.lbm_grid_neighbors(h, nghbr.ctypes.data), what="lbm_grid_neighbors")
     finally:
         lib.lbm_grid_destroy(h)
+    extra = dict(level=tree_level, nchildren=tree_nchildren, partition_lvl=int(pl.value), highest_lvl=int(hl.value)) if multilevel else {}
     return GridTables(ndim=ndim, centers=centers, nghbr=nghbr, surfaces=surfaces, bbox=box, cell_length=float(cl.value),
-                      max_lvl=level)
+                      max_lvl=level, **extra)
 
 
 @dataclass

@@ -78,10 +78,42 @@ class GridTables:
     bbox: np.ndarray  # (2*ndim,) min0,max0,min1,max1,...
     cell_length: float
     max_lvl: int
+    # multi-level grids (every level of the generator's array): each cell's
+    # level and number of children; None for a uniform grid
+    level: Optional[np.ndarray] = None
+    nchildren: Optional[np.ndarray] = None
+    partition_lvl: Optional[int] = None
+    highest_lvl: Optional[int] = None
 
     @property
     def ncells(self) -> int:
         return int(self.centers.shape[0])
+
+    def output_cells(self, solver: Optional[dict] = None) -> np.ndarray:
+        """The cells the solution output writes: the solver's "cellFilter"
+        (default "leafCells"; CellFilterManager, src/cell_filter.h:57-110:
+        "leafCells", "highestLvl", "lowestLvl" / "partitionLvl", "targetLvl"
+        with "outputLvl"), in cell order.  Every cell of a uniform grid."""
+        if self.level is None:
+            return np.arange(self.ncells)
+        conf = (solver or {}).get("cellFilter", {"cellFilter": "leafCells"})
+        kind = conf.get("cellFilter") if isinstance(conf, dict) else None
+        lv = self.level.astype(np.int64)
+        if kind == "leafCells":
+            keep = self.nchildren == 0
+        elif kind == "highestLvl":
+            keep = lv == int(self.highest_lvl)
+        elif kind in ("lowestLvl", "partitionLvl"):
+            keep = lv == int(self.partition_lvl)
+        elif kind == "targetLvl":
+            if "outputLvl" not in conf:
+                raise ConfigError('"targetLvl" needs "outputLvl"')
+            if int(conf["outputLvl"]) < int(self.partition_lvl):
+                raise ConfigError("Outputting a lvl below the partition lvl is not possible!")
+            keep = lv == int(conf["outputLvl"])
+        else:
+            raise ConfigError(f"Unknown output filter {kind}")
+        return np.flatnonzero(keep)
 
 
 @dataclass

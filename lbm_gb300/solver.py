@@ -463,7 +463,9 @@ class LBMSolver:
     def write_solution(self, path: str) -> str:
         """``output`` (src/lbm/solver.cpp:322-384): recompute the moments and
         write the reference's VTK PolyData file (U, V, rho or the potential V
-        at the cell centres)."""
+        at the cell centres) for the cells the solver's "cellFilter" passes
+        (every cell of a uniform grid; the leaf cells of a multi-level one by
+        default, src/lbm/solver.cpp:86)."""
         from .output import solution_arrays, write_vtp
 
         self.gpu.update_moments()
@@ -473,7 +475,10 @@ class LBMSolver:
             arrays = solution_arrays(grid.ndim, rho=v[:, grid.ndim], u=[v[:, d] for d in range(grid.ndim)])
         else:
             arrays = solution_arrays(grid.ndim, phi=v[:, 0])
-        return write_vtp(path, grid.centers.reshape(grid.ncells, grid.ndim), arrays)
+        keep = grid.output_cells(self.cfg)
+        if keep.size != grid.ncells:
+            arrays = [(name, a[keep]) for name, a in arrays]
+        return write_vtp(path, grid.centers.reshape(grid.ncells, grid.ndim)[keep], arrays)
 
     def write_line(self, path: str, a, b) -> str:
         """A line probe of the reference's post-processing

@@ -116,7 +116,7 @@ def run_case(name, src, steps):
 
 # cases whose final state the reference also writes through its own VTK
 # output (LBMSolver::output, binary PolyData): tests/golden/<case>_<steps>_ref.vtp
-VTP_CASES = [("cavity_small", 100), ("poisson2d_helmholtz_small", 100)]
+VTP_CASES = [("cavity_small", 100), ("poisson2d_helmholtz_small", 100), ("cavity_p2u3m5", 100)]
 
 
 def run_vtp(name, steps):

@@ -47,8 +47,16 @@ def _tags(text):
     return [re.sub(r"\s+", " ", t).strip() for t in re.findall(r"<[^>]+>", text)]
 
 
-@pytest.mark.parametrize("name", ["cavity_small_100", "poisson2d_helmholtz_small_100"])
+@pytest.mark.parametrize("name", ["cavity_small_100", "poisson2d_helmholtz_small_100", "cavity_p2u3m5_100"])
 def test_matches_reference_vtk_output(name, tmp_path):
+    """The solution file of the reference's output (src/lbm/solver.cpp:322-384)
+    from the oracle's state: array for array, and tag for tag.  On the
+    multi-level grid (cavity_p2u3m5) the file holds the leaf cells only, the
+    solver's default "cellFilter" (GridTables.output_cells)."""
+    import json
+
+    from lbm_gb300 import gridgen
+
     meta, solver, grid, out = caseio.load(name)
     consts = rc.solver_constants(solver, grid)
     bnds = rc.boundary_list(solver, grid, consts)
@@ -61,7 +69,11 @@ def test_matches_reference_vtk_output(name, tmp_path):
         arrays = solution_arrays(grid.ndim, rho=v[:, grid.ndim], u=[v[:, d] for d in range(grid.ndim)])
     else:
         arrays = solution_arrays(grid.ndim, phi=v[:, 0])
-    mine = write_vtp(str(tmp_path / "solution"), grid.centers.reshape(grid.ncells, grid.ndim), arrays)
+    configs = json.load(open(os.path.join(GOLD, "grid_configs.json")))
+    keep = gridgen.grid_tables(configs[name.rsplit("_", 1)[0]]).output_cells(solver)
+    assert (keep.size < grid.ncells) == (name == "cavity_p2u3m5_100")
+    arrays = [(k, a[keep]) for k, a in arrays]
+    mine = write_vtp(str(tmp_path / "solution"), grid.centers.reshape(grid.ncells, grid.ndim)[keep], arrays)
     ref = os.path.join(GOLD, f"{name}_ref.vtp")
     p0, a0 = read_vtp(ref)
     p1, a1 = read_vtp(mine)

@@ -154,6 +154,31 @@ def test_solution_output_matches_reference_file(name, tmp_path):
         assert np.array_equal(a0[k], a1[k]), k
 
 
+def test_multilevel_solution_output_matches_reference_file(tmp_path):
+    """On a multi-level grid built from its JSON config (levels 2, 3 and
+    boundary cells to 5), write_solution writes the leaf cells, the solver's
+    default "cellFilter", as the reference's own file does."""
+    import json
+    import os
+
+    from lbm_gb300.output import read_vtp
+    from lbm_gb300.solver import LBMSolver
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    cfg = json.load(open(os.path.join(here, "golden", "grid_configs.json")))["cavity_p2u3m5"]
+    meta, solver, _, _, _, _, _ = load_case("cavity_p2u3m5_100")
+    s = LBMSolver.from_config(dict(cfg, solver=solver))
+    s.gpu.initial_condition()
+    s.gpu.step(meta["steps"])
+    mine = s.write_solution(str(tmp_path / "solution"))
+    p0, a0 = read_vtp(os.path.join(here, "golden", "cavity_p2u3m5_100_ref.vtp"))
+    p1, a1 = read_vtp(mine)
+    assert p0.shape[0] < meta["cells"]
+    assert np.array_equal(p0, p1) and sorted(a0) == sorted(a1)
+    for k in a0:
+        assert np.array_equal(a0[k], a1[k]), k
+
+
 LINES = [
     ("cavity_small", 100, "x0p53", [0.53125, 0.0], [0.53125, 1.0]),
     ("cavity_small", 100, "diag", [0.0, 0.0], [1.0, 1.0]),
