@@ -420,12 +420,25 @@ int ora_add_bnd(ora_ctx* c, int kind, int64_t ncells, const int64_t* cells, cons
         b->ext[i]     = NB(c, cells[i], od);
         b->ext_dir[i] = od;
         if(b->ext[i] == INVALID) return -3;
+        /* the Neumann value extrapolates from a second cell further in; a
+           grid without it (refined grids can lack it) is refused, as the
+           library's table upload refuses it */
+        if(kind == ORA_BND_NEUMANN_NEEM && NB(c, b->ext[i], od) == INVALID) return -3;
       }
       break;
     }
+    case ORA_BND_PRESSURE_ABB:
+      /* the extrapolation reads the two cells inside the boundary cell
+         (bnd_pressure.h:73-78); the reference does not check that they
+         exist, here a grid without them is refused */
+      for(int64_t i = 0; i < ncells; ++i) {
+        const int     id = inside_dir(&normals[i * D], D);
+        const int64_t n1 = id < 0 ? INVALID : NB(c, cells[i], id);
+        if(n1 == INVALID || NB(c, n1, id) == INVALID) return -3;
+      }
+      break;
     case ORA_BND_WALL_BB:
     case ORA_BND_DIRICHLET_BB:
-    case ORA_BND_PRESSURE_ABB:
       break;
     default:
       return -1;
