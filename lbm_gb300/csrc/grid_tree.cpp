@@ -294,10 +294,8 @@ using namespace lbm_grid_impl;
 
 extern "C" {
 
-int lbm_grid_tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_level, int32_t max_level, int64_t max_cells,
-                         const lbm_geom_desc* objs, int32_t nobj, const double* bbox, int32_t align_dir, lbm_grid_tree** out) {
-  if(!out) return LBM_ERR_INVALID;
-  *out = nullptr;
+static int tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_level, int32_t max_level, int64_t max_cells,
+                       const lbm_geom_desc* objs, int32_t nobj, const double* bbox, int32_t align_dir, lbm_grid_tree** out) {
   if(partition_level < 0 || partition_level > uniform_level || uniform_level > max_level || max_level > 20 || max_cells < 1)
     return LBM_ERR_INVALID;
   if(align_dir >= ndim) return LBM_ERR_INVALID;
@@ -473,6 +471,17 @@ int lbm_grid_tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_
   return LBM_OK;
 }
 
+int lbm_grid_tree_create(int32_t ndim, int32_t partition_level, int32_t uniform_level, int32_t max_level, int64_t max_cells,
+                         const lbm_geom_desc* objs, int32_t nobj, const double* bbox, int32_t align_dir, lbm_grid_tree** out) {
+  if(!out) return LBM_ERR_INVALID;
+  *out = nullptr;
+  try {
+    return tree_create(ndim, partition_level, uniform_level, max_level, max_cells, objs, nobj, bbox, align_dir, out);
+  } catch(const std::bad_alloc&) {  // no exception crosses the C boundary
+    return LBM_ERR_NOMEM;
+  }
+}
+
 int64_t lbm_grid_tree_ncells(const lbm_grid_tree* t) { return t ? t->n : 0; }
 
 int lbm_grid_tree_levels(const lbm_grid_tree* t, int32_t* partition_level, int32_t* highest_level) {
@@ -571,11 +580,11 @@ int lbm_grid_tree_grid(const lbm_grid_tree* t, lbm_grid** out) {
       for(int dir = 0; dir < nn; ++dir) present += g->nbr[c * nn + dir] >= 0 ? 1 : 0;
       g->bndry[c] = present < nn ? 1 : 0;
     }
+    list_boundary_cells(*g);
   } catch(const std::bad_alloc&) {
     delete g;
     return LBM_ERR_NOMEM;
   }
-  list_boundary_cells(*g);
   *out = g;
   return LBM_OK;
 }
