@@ -75,6 +75,7 @@ struct ora_box {
   int      has_force;
   double   inlet_u[3], inlet_rho;
   double   kappa_sq;
+  double*  slice_kappa; /* nz values of kappa^2 (one per z-slice) or NULL: kappa_sq */
   int      nonlinear;
   double*  dirichlet;
   int      dev;  /* Navier-Stokes state held as deviations f - w (see ora_box_set_deviation) */
@@ -124,9 +125,21 @@ void ora_box_destroy(ora_box* b) {
   if(!b) return;
   free(b->flags);
   free(b->dirichlet);
+  free(b->slice_kappa);
   free(b->f);
   free(b->fs);
   free(b);
+}
+
+/* a kappa^2 per z-slice (nz values; NULL: the box's single kappa^2), the
+   engine's lbm_gpu_box_set_slice_kappa */
+int ora_box_set_slice_kappa(ora_box* b, const double* kappa_sq) {
+  free(b->slice_kappa);
+  b->slice_kappa = NULL;
+  if(!kappa_sq) return 0;
+  b->slice_kappa = (double*)malloc(sizeof(double) * b->n[2]);
+  memcpy(b->slice_kappa, kappa_sq, sizeof(double) * b->n[2]);
+  return 0;
 }
 
 int ora_box_set_poisson(ora_box* b, double kappa_sq, int nonlinear, const double* phi) {
@@ -194,7 +207,7 @@ static void emit(const ora_box* b, int64_t cell, double* out) {
   }
 }
 
-static void collide_cell(const ora_box* b, const double* f, double* out) {
+static void collide_cell(const ora_box* b, const double* f, double* out, int z) {
   const blat_t* L = &b->L;
   const int     Q = L->Q, D = L->D;
   const double  om = b->omega;
@@ -232,7 +245,7 @@ static void collide_cell(const ora_box* b, const double* f, double* out) {
     for(int q = 0; q < Q; ++q) {
       const double feq = q == Q - 1 ? (L->w[Q - 1] - 1.0) * phi : L->w[q] * phi;
       double       o   = f[q] + om * (feq - f[q]);
-      if(q != Q - 1) o += L->pw[q] * diff * b->kappa_sq * g;
+      if(q != Q - 1) o += L->pw[q] * diff * (b->slice_kappa ? b->slice_kappa[z] : b->kappa_sq) * g;
       out[q] = o;
     }
   }
@@ -301,7 +314,7 @@ void ora_box_step(ora_box* b, int64_t nsteps, int nthreads) {
         emit(b, cell, o);
       } else {
         for(int q = 0; q < Q; ++q) f[q] = b->f[q * N + cell];
-        collide_cell(b, f, o);
+        collide_cell(b, f, o, (int)(cell / ((int64_t)b->n[0] * b->n[1])));
       }
       for(int q = 0; q < Q; ++q) b->fs[q * N + cell] = o[q];
     }

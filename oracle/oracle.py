@@ -63,6 +63,8 @@ def lib():
         L.ora_box_destroy.argtypes = [vp]
         L.ora_box_set_poisson.argtypes = [vp, dbl, i32, vp]
         L.ora_box_set_poisson.restype = i32
+        L.ora_box_set_slice_kappa.argtypes = [vp, vp]
+        L.ora_box_set_slice_kappa.restype = i32
         L.ora_box_init_equilibrium.argtypes = [vp, dbl, vp]
         L.ora_box_step.argtypes = [vp, i64, i32]
         L.ora_box_get.argtypes = [vp, vp, vp, vp]
@@ -176,6 +178,12 @@ class BoxOracle:
         if getattr(self, "h", None):
             lib().ora_box_destroy(self.h)
             self.h = None
+
+    def set_slice_kappa(self, kappa_sq):
+        """One kappa^2 per z-slice (Poisson-Boltzmann; None: the box's single
+        kappa^2), as lbm_gpu_box_set_slice_kappa."""
+        k = None if kappa_sq is None else np.ascontiguousarray(kappa_sq, dtype=np.float64)
+        lib().ora_box_set_slice_kappa(self.h, _p(k))
 
     def init_equilibrium(self, rho=1.0, u=(0, 0, 0)):
         uu = np.asarray(u, dtype=np.float64)

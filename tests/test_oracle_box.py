@@ -84,3 +84,32 @@ def test_even_periodic_channel_can_keep_a_period_two_mode():
     assert one > 1e-5 and two < 1e-10
     one_odd, _ = _one_and_two_step_change(127)
     assert one_odd < 1e-7
+
+
+def test_debye_sweep_boxes_are_independent():
+    """A Debye-length sweep as the engine runs it (lbm_gpu_box_set_slice_kappa):
+    charged-sphere boxes of different Debye lengths, each closed by Dirichlet
+    planes, stacked along z with a kappa^2 per z-slice.  In the oracle each
+    stacked box steps bit for bit as a box of its own: the Dirichlet planes
+    emit their own equilibrium whatever they receive, so nothing crosses."""
+    from lbm_gb300 import cases
+
+    units = [cases.pb_spheres(n=16, seed=s, count=1) for s in (3, 5, 9)]
+    assert len({u["kappa_sq"] for u in units}) == 3
+    st = cases.stacked_debye(units)
+    o = oracle.BoxOracle(st["lattice"], st["shape"], st["omega"], pb_nonlinear=True, **cases.box_kwargs(st))
+    o.set_slice_kappa(st["slice_kappa_sq"])
+    o.init_equilibrium()
+    o.step(30)
+    f = o.populations()
+    n3 = 16 ** 3
+    for k, u in enumerate(units):
+        one = oracle.BoxOracle(u["lattice"], u["shape"], u["omega"], pb_nonlinear=True, **cases.box_kwargs(u))
+        one.init_equilibrium()
+        one.step(30)
+        assert np.array_equal(f[:, k * n3:(k + 1) * n3], one.populations()), k
+    # one kappa^2 for every slice again: the stack differs from the sweep
+    o.set_slice_kappa(None)
+    o.init_equilibrium()
+    o.step(30)
+    assert not np.array_equal(o.populations()[:, n3:2 * n3], f[:, n3:2 * n3])
