@@ -220,7 +220,7 @@ def accuracy_run(args):
     out = {"metric": "velocity relative L2 vs FP64 (D3Q19 sphere)", "unit": "relative L2", "higher_is_better": False,
            "dtype": "f64 reference; f32 / f16 / bf16 storage with f32 arithmetic", "data": "synthetic", "rows": []}
     spec = {"f64": ("f64", True), "f32": ("f32", True), "f32_noshift": ("f32", False), "f16dev": ("f16dev", True),
-            "f16dev_noshift": ("f16dev", False), "bf16dev": ("bf16dev", True)}
+            "f16dev_noshift": ("f16dev", False), "bf16dev": ("bf16dev", True), "e3m12dev": ("e3m12dev", True)}
     runs = (((256, 128, 128, 12.0, (64.0, 64.0, 64.0)), (1000, 5000, 20000, 50000)),
             ((512, 256, 256, 24.0, (128.0, 128.0, 128.0)), (2000, 5000, 10000)))
     if args.acc_full_steps:
