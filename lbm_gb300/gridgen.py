@@ -140,8 +140,12 @@ def geometry_objects(geometry: Dict, ndim: int):
 
 def grid_tables(config: Dict, device: Optional[int] = None) -> GridTables:
     """The reference's LBM grid tables for a JSON config (the grid generator's
-    keys plus ``solver.boundary``).  With ``device`` the cells are enumerated
-    on that GPU (``lbm_grid_create_device``, the same tables)."""
+    keys plus ``solver.boundary``).  With ``device`` the cells of a uniform
+    grid are enumerated on that GPU (``lbm_grid_create_device``, the same
+    tables); a multi-level grid (levels not all equal) is built on the host
+    from the generator's tree (``lbm_grid_tree_grid``) either way, and its
+    tables carry each cell's level and child count (``GridTables.level``,
+    ``nchildren``)."""
     ndim = int(config.get("dim", 0))
     if ndim not in (1, 2, 3):
         raise ConfigError(f"dim must be 1, 2 or 3, got {ndim}")
