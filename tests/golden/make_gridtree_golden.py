@@ -37,6 +37,10 @@ CHANNEL = {"cube": {"type": "box", "body": "flowregion", "A": [0.0, 0.0], "B": [
            "sphere": {"type": "sphere", "body": "flowregion", "subtract": True, "center": [3.1, 2.05], "radius": 0.8}}
 
 
+HOLE = {"cube": {"type": "box", "body": "f", "A": [0.0, 0.0], "B": [3.0, 1.0]},
+        "hole": {"type": "sphere", "body": "f", "subtract": True, "center": [1.1, 0.45], "radius": 0.2}}
+
+
 def levels(p, u, m, cells=400000):
     return {"partitionLevel": p, "uniformLevel": u, "maxRfnmtLvl": m, "maxNoCells": cells}
 
@@ -63,6 +67,11 @@ CASES = [
     # the reference's 2D Poisson square with its alignNodesWithSurface
     ("poisson2D_p2u3m6", ("ref", "test/poisson/poisson2D.json"), levels(2, 3, 6)),
     ("poisson2D_l5", ("ref", "test/poisson/poisson2D.json"), levels(5, 5, 5)),
+    # partitioning levels 0 and 1 (the root itself, or its children, in
+    # curve order), and a uniform multi-level grid stretched by the alignment
+    ("hole_p0u3m5", ("own", {"dim": 2, "geometry": HOLE}), levels(0, 3, 5)),
+    ("hole_p1u1m4", ("own", {"dim": 2, "geometry": HOLE}), levels(1, 1, 4)),
+    ("hole_p2u5_align", ("own", {"dim": 2, "geometry": HOLE, "alignNodesWithSurface": True}), levels(2, 5, 5)),
 ]
 
 

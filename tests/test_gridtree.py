@@ -8,10 +8,10 @@ cell's centre, level, parent, global id, children, same-level neighbours and
 boundary property, and the points file the generator wrote.
 lbm_gb300.gridgen.grid_tree builds the tree from the config alone; it must be
 equal bit for bit, and save_grid must write the same file byte for byte.
-The cases cover odd and even partitioning levels, uniform refinement finer
-than the partitioning level, boundary refinement, alignNodesWithSurface on a
-refined grid, disjoint regions, 1D, and two of the reference's own test
-geometries.  All host-only: no GPU.
+The cases cover partitioning levels 0 to 3 (odd and even), uniform
+refinement finer than the partitioning level, boundary refinement,
+alignNodesWithSurface on refined and on uniform multi-level grids, disjoint
+regions, 1D, and two of the reference's own test geometries.  All host-only: no GPU.
 """
 import glob
 import json
@@ -35,7 +35,7 @@ def load(name):
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 9
+    assert len(FIXTURES) >= 12
 
 
 @pytest.mark.parametrize("name", FIXTURES)
