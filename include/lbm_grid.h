@@ -21,6 +21,12 @@
  *                                (src/cartesiangrid.h:551-598)
  *   lbm_grid_connect_periodic    CartesianGrid::addPeriodicConnection (src/cartesiangrid.h:636-703)
  *   lbm_grid_neighbors           the neighbour table after addDiagonalNghbrs (src/cartesiangrid.h:450-487)
+ *   lbm_grid_tree_create         GridGenerator::generateGrid for any partitionLevel <= uniformLevel <=
+ *                                maxRfnmtLvl (src/gridgenerator/gridGenerator.cpp:163-238,
+ *                                src/gridgenerator/cartesiangrid_generation.h)
+ *   lbm_grid_tree_write_points   CartesianGridGen::save, ASCII points (cartesiangrid_generation.h:208-253)
+ *   lbm_grid_tree_grid           CartesianGrid::loadGridInplace of the whole array, boundary cells included
+ *                                (src/cartesiangrid.h:264-320, 509-544)
  *
  * In 2D (and 1D) every table equals the reference's bit for bit.  In 3D,
  * where the reference stops (box and sphere cut tests, src/geometry.h:690-692
